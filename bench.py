@@ -1,0 +1,357 @@
+"""Benchmark of the D3Q19 hot path on GB300 (one JSON line on stdout).
+
+Workload (the reference-derived plain configuration at scale): lid-driven
+cavity, 256^3 cells decomposed into 2x2x1 subdomains of 128x128x256 held on
+one GPU, D3Q19 BGK + Smagorinsky (Cs 0.17), Re 10000 on lid length 256, lid
+speed 0.1, FP32 populations, seeded start-up velocity uniform on +-1e-3
+(Philox, seed 1234).  A "step" is one time step of the whole domain: the
+alternating beta/alpha step kernel over all four subdomains plus the CComm
+halo exchange in x, y, z order (CController::computeNextStep).
+
+Reported:
+  value      MLUPS over all cells (walls and ghost layers included, the
+             reference's count), device-resident fields, timed with CUDA
+             events on the launching stream around K steps;
+  roofline   the step kernel against the measured HBM copy bandwidth;
+             algorithmic bytes = 2*19*4 = 152 per cell update;
+  e2e        the same metric through the C ABI with host buffers: upload of
+             the initial populations from pinned host memory, K steps, and
+             the final velocity field read back to the host, all timed;
+  cpu_baseline  the oracle port of the reference kernels on the host cores.
+
+--impl reference times the CPU implementation (the oracle port of the
+reference's kernels, all host threads) on the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "D3Q19 MLUPS & % HBM roofline; served solves/s, p50/p99 latency vs plain"
+SIZE = (256, 256, 256)
+NUMS = (2, 2, 1)
+U_LID, RE, CS, SEED, AMP = 0.1, 10000.0, 0.17, 1234, 1e-3
+BYTES_PER_CELL = {"f32": 152, "f64": 304, "f16": 76, "bf16": 76}
+
+
+def lattice_params(dtype):
+    import numpy as np
+
+    tau = 3.0 * U_LID * SIZE[0] / RE + 0.5
+    t = dtype(tau)
+    return dict(inv_tau=float(dtype(1) / t), tau0=float(t),
+                les_c=float(dtype(18.0 * math.sqrt(2.0) * CS * CS)), lid=float(dtype(U_LID)))
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, backend):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group(backend=backend)
+        return dist
+    return None
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per cell update of the step kernel from the committed ncu
+    summary (profiles/roofline_inputs.txt), or None."""
+    f = ROOT / "profiles" / "roofline_inputs.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_cell_update_f32:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except Exception:
+                self.proc.kill()
+            self.t.join(1)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------ CPU (oracle)
+def cpu_run(cells_z: int, steps: int, warmup: int, threads: int):
+    """Oracle port of the reference kernels on the host cores, same
+    configuration with a shorter z extent; returns (MLUPS, seconds, cells)."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import numpy as np
+
+    from oracle import oracle as O
+
+    size = (SIZE[0], SIZE[1], cells_z)
+    pp = lattice_params(np.float32)
+    p = O.Params(inv_tau=pp["inv_tau"], tau0=pp["tau0"], les_c=pp["les_c"], lid=pp["lid"],
+                 store_vel=False, store_rho=False)
+    D = O.Domain(lambda d: O.OracleKernels("f32"), size, NUMS, p, "f32")
+    D.perturb(SEED, AMP)
+    for _ in range(warmup):
+        D.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        D.step()
+    dt = time.perf_counter() - t0
+    cells = size[0] * size[1] * size[2]
+    return cells * steps / dt / 1e6, dt, cells
+
+
+def cpu_baseline_sample():
+    threads = os.cpu_count() or 1
+    z = 16
+    mlups, dt, cells = cpu_run(z, 4, 1, threads)
+    return {"value": round(mlups, 2), "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"oracle port (C, OpenMP) of the reference kernels, 256x256x{z} slab of the same "
+                      f"2x2x1 cavity config, 4 timed steps after 1 warm-up ({dt:.1f} s)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # calibrate so that warm-up + timed steps take about 90 s in total
+    m0, _, _ = cpu_run(8, 2, 1, threads)
+    per_cell_s = 1.0 / (m0 * 1e6)
+    budget = 90.0 / max(1, args.steps + args.warmup)
+    z = int(max(6, min(SIZE[2], budget / (per_cell_s * SIZE[0] * SIZE[1]))))
+    mlups, dt, cells = cpu_run(z, args.steps, args.warmup, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict("reference CPU arm: same cavity, z extent %d per step sample" % z),
+        "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"256x256x{z} slab of the 2x2x1 cavity per step ({cells} cells)"},
+        "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(note=None):
+    d = {"workload": "lid-driven cavity 256^3, 2x2x1 subdomains of 128x128x256 on one GPU, D3Q19 BGK + "
+                     "Smagorinsky Cs=0.17, Re=10000, lid u=0.1, seeded start-up +-1e-3",
+         "size": list(SIZE), "subdomains": list(NUMS), "storage": "f32", "cs": CS, "re": RE, "lid": U_LID,
+         "l2": "inputs larger than L2 (1.27 GB of populations per step vs 129 MB L2)"}
+    if note:
+        d["note"] = note
+    return d
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    ws, rank, local = dist_env()
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = init_dist(ws, "nccl")
+    from turbulent_lbm_multigpu_gb300 import build, capi as api
+
+    if rank == 0 or not build.LIB.exists():
+        build.build()
+    if dist:
+        dist.barrier()
+    pp = lattice_params(np.float32)
+    prm = api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
+
+    D = api.Domain(SIZE, NUMS, api.F32, store_velocity=False, store_density=False)
+    D.set_params(prm)
+    D.reset()
+    D.perturb(SEED, AMP)
+    D.run(args.warmup, use_graph=False)
+    torch.cuda.synchronize()
+
+    # timed region: eager steps with one CUDA-event pair around every step kernel
+    D.profile(True)
+    D.kernel_time(reset=True)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record()
+        D.run(args.steps, use_graph=False)
+        stop.record()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = start.elapsed_time(stop)
+    k_ms, k_n = D.kernel_time(reset=True)
+    D.profile(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cells = D.cells
+    mlups = cells * args.steps * ws / (ms * 1e-3) / 1e6
+
+    # the same with CUDA-graph replay of step pairs
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    D.run(args.steps, use_graph=True)
+    g1.record()
+    torch.cuda.synchronize()
+    graph_mlups = cells * args.steps / (g0.elapsed_time(g1) * 1e-3) / 1e6
+
+    # roofline of the step kernel
+    peak, peak_kind = measured_peak()
+    per_launch_ms = k_ms / max(1, k_n)
+    alg_bytes = BYTES_PER_CELL["f32"] * cells
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = profiled_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": round(traffic * cells) if traffic else None,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                "fallback 6.8 TB/s", "kernel": "k_beta/k_alpha<float,LES> (step kernel)",
+                "kernel_ms_per_launch": round(per_launch_ms, 4), "alg_bytes_per_launch": alg_bytes}
+    del D
+
+    # e2e through the C ABI with host buffers
+    e2e = run_e2e(api, prm, args.steps)
+
+    line = {
+        "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict(), "roofline": roofline, "e2e": e2e,
+        "gpu_launches": int(args.steps * (1 + 2)),
+        "clocks": clk.summary(),
+        "graph_mlups": round(graph_mlups, 1),
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_e2e(api, prm, steps):
+    """Upload the start-up field from pinned host memory, run, read the velocity back."""
+    import numpy as np
+    import torch
+
+    D = api.Domain(SIZE, NUMS, api.F32, store_velocity=True, store_density=False)
+    D.set_params(prm)
+    D.reset()
+    D.perturb(SEED, AMP)
+    D.set_store_interval(0)  # velocity written on the last step only
+    sub = D.sub
+    n = sub[0] * sub[1] * sub[2]
+    host_in = [torch.empty(19 * n, dtype=torch.float32).pin_memory().numpy() for _ in D.subdomains]
+    host_out = [torch.empty(3 * n, dtype=torch.float32).pin_memory().numpy() for _ in D.subdomains]
+    for L, h in zip(D.subdomains, host_in):
+        L.read(api.FIELD_DD, out=h.reshape(19, sub[2], sub[1], sub[0]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for L, h in zip(D.subdomains, host_in):
+        L.write(api.FIELD_DD, h)
+    D.run(steps, use_graph=True)
+    for L, h in zip(D.subdomains, host_out):
+        L.read(api.FIELD_VELOCITY, out=h.reshape(3, sub[2], sub[1], sub[0]))
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    h2d = sum(h.nbytes for h in host_in)
+    d2h = sum(h.nbytes for h in host_out)
+    del D
+    return {"value": round(D_cells() * steps / (ms * 1e-3) / 1e6, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": int(h2d // steps), "d2h_bytes_per_step": int(d2h // steps),
+            "wall_s": round(wall, 4),
+            "note": "start-up populations uploaded once and velocity read once per run of `steps` steps; "
+                    "bytes per step are those totals divided by the step count"}
+
+
+def D_cells():
+    return SIZE[0] * SIZE[1] * SIZE[2]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

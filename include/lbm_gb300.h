@@ -1,0 +1,169 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300 D3Q19 lattice Boltzmann hot path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, status codes.  Every
+ * function returns 0 on success and a negative value on failure, with the
+ * message available from lbm_cu_last_error() on the calling thread.
+ * `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Host buffers are caller-owned and caller-sized, as in the reference.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the reference project).  The reference compiles OpenCL programs per
+ * domain size at run time and launches them through CCL; here the kernels
+ * are compiled once for sm_103a and take sizes at run time.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Cell flags: src/CLbmSolver.hpp:30-33 (src/common.h:19-22). */
+#define LBM_FLAG_OBSTACLE 1
+#define LBM_FLAG_FLUID 2
+#define LBM_FLAG_VELOCITY_INJECTION 4
+#define LBM_FLAG_GHOST_LAYER 8
+
+/* Population storage.  F32/F64 correspond to the reference's T = float /
+ * double.  F16/BF16 store the shifted deviations f_i - w_i and compute in
+ * float (no reference counterpart). */
+enum lbm_storage { LBM_F32 = 0, LBM_F64 = 1, LBM_F16 = 2, LBM_BF16 = 3 };
+
+/* Fields for rectangular reads and writes. */
+enum lbm_field {
+    LBM_FIELD_DD = 0,       /* 19 population planes */
+    LBM_FIELD_VELOCITY = 1, /* 3 planes: the momentum sum_i e_i f_i */
+    LBM_FIELD_DENSITY = 2,  /* 1 plane */
+    LBM_FIELD_FLAGS = 3     /* 1 plane of int32 on the host */
+};
+
+/* Kernel arguments, given in double and rounded to the arithmetic type.
+ * inv_tau, gravity and lid are the reference kernel arguments
+ * (src/CLbmSolver.hpp:593-612).  les_c = 18*sqrt(2)*Cs^2 switches on the
+ * Smagorinsky subgrid model (0 = off, the reference's plain BGK) and tau0 is
+ * the molecular relaxation time it builds on. */
+typedef struct lbm_params {
+    double inv_tau;
+    double tau0;
+    double les_c;
+    double gravity[3];
+    double lid;
+} lbm_params;
+
+typedef struct lbm_lattice lbm_lattice; /* one subdomain's device fields */
+typedef struct lbm_domain lbm_domain;   /* a decomposed domain on one GPU */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *lbm_cu_last_error(void);
+
+/* Library build string (kernels, architecture, compile options). */
+const char *lbm_cu_version(void);
+
+/* ---------------------------------------------------------------- lattice */
+
+/* Allocate the fields of one nx*ny*nz lattice on the current device.
+ * Replaces the buffer creation of CLbmSolver::reload
+ * (src/CLbmSolver.hpp:381-403).  Velocity and density planes exist only when
+ * requested, like STORE_VELOCITY / STORE_DENSITY (src/CLbmSolver.hpp:369-373). */
+int lbm_cu_create(int nx, int ny, int nz, int storage, int store_velocity, int store_density,
+                  lbm_lattice **out);
+int lbm_cu_destroy(lbm_lattice *lat);
+int lbm_cu_dims(const lbm_lattice *lat, int dims[3]);
+
+/* Set the kernel arguments.  Replaces the setArg calls of
+ * CLbmSolver::reload / addDrivenCavityValue (src/CLbmSolver.hpp:592-612,262-270). */
+int lbm_cu_set_params(lbm_lattice *lat, const lbm_params *p);
+
+/* init_kernel (src/cl_programs/lbm_init.cl:32-237), enqueued by
+ * CLbmSolver::reset (src/CLbmSolver.hpp:619-635): flags from the six face
+ * conditions bc = {x-, x+, y-, y+, z-, z+}, rest equilibrium, u = 0, rho = 1. */
+int lbm_cu_init(lbm_lattice *lat, const int bc[6], void *stream);
+
+/* Seeded start-up field (no reference counterpart): every cell strictly
+ * inside the physical domain gets eq(rho = 1, u) with u uniform on
+ * [-amp, amp) per component from Philox4x32-10 keyed by (seed, physical cell
+ * index), stored in the slot order the first (beta) step reads.
+ * origin = physical position of cell (0,0,0), phys = physical domain size. */
+int lbm_cu_perturb(lbm_lattice *lat, const int origin[3], const int phys[3], uint64_t seed,
+                   double amp, void *stream);
+
+/* One step: parity 0 = lbm_kernel_beta (src/cl_programs/lbm_beta.cl),
+ * parity 1 = lbm_kernel_alpha (src/cl_programs/lbm_alpha.cl).  Replaces
+ * CLbmSolver::simulationStepBeta / simulationStepAlpha
+ * (src/CLbmSolver.hpp:637-659); the caller keeps the step counter like
+ * CLbmSolver::simulationStep (src/CLbmSolver.hpp:664-676). */
+int lbm_cu_step(lbm_lattice *lat, int parity, void *stream);
+
+/* Rectangular copy of one field between the lattice and a HOST buffer laid
+ * out [plane][z][y][x] of size[0]*size[1]*size[2] cells per plane, elements
+ * of the arithmetic type (float for F32/F16/BF16, double for F64) or int32
+ * for flags.  Blocking, like the reference's CL_TRUE reads.  Replaces
+ * storeDensityDistribution / storeVelocity / storeDensity / storeFlags and
+ * their set* counterparts, with or without a rectangle
+ * (src/CLbmSolver.hpp:688-978).  For writes of LBM_FIELD_DD, `norm` (may be
+ * NULL) restricts the copy to populations f with norm . e_f > 0, as the
+ * masked setDensityDistribution (src/CLbmSolver.hpp:738-757). */
+int lbm_cu_read(lbm_lattice *lat, int field, const int origin[3], const int size[3], void *host_dst,
+                void *stream);
+int lbm_cu_write(lbm_lattice *lat, int field, const int origin[3], const int size[3],
+                 const void *host_src, const int norm[3], void *stream);
+
+/* Device-to-device CComm exchange between two lattices of the same storage
+ * (no host staging): dst[dst_origin + box] = src[src_origin + box] for every
+ * population plane, or only for those with norm . e_f > 0 when norm is not
+ * NULL.  Replaces one storeDensityDistribution -> MPI -> setDensityDistribution
+ * round trip of CController::syncAlpha / syncBeta (src/CController.hpp:265-383). */
+int lbm_cu_halo(lbm_lattice *src, const int src_origin[3], lbm_lattice *dst, const int dst_origin[3],
+                const int size[3], const int norm[3], void *stream);
+
+/* FP64 compensated (Neumaier) sums over fluid cells of mass, momentum and
+ * kinetic energy of the populations currently stored: out = {sum rho,
+ * sum jx, sum jy, sum jz, sum |j|^2/2}.  `layout` 0: standard slots (after a
+ * beta step), 1: opposite slots (after an alpha step or the seeded start-up).
+ * No reference counterpart. */
+int lbm_cu_reduce_conserved(lbm_lattice *lat, int layout, double out[5], void *stream);
+
+/* ----------------------------------------------------------------- domain */
+
+/* A decomposed domain held on one GPU: the even split and CComm geometry of
+ * CManager::initSimulation (src/CManager.hpp:49-204) for every subdomain at
+ * once, the lid plane of CController::setGeometry (src/CController.hpp:531-546)
+ * in the top row of subdomains when lid_geometry != 0, and halo exchanges as
+ * device-local copies.  Subdomain i has coordinates (i % nx, i / nx % ny,
+ * i / (nx*ny)) like the reference's rank mapping. */
+int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int store_velocity,
+                         int store_density, int lid_geometry, lbm_domain **out);
+int lbm_cu_domain_destroy(lbm_domain *dom);
+int lbm_cu_domain_set_params(lbm_domain *dom, const lbm_params *p);
+/* init + geometry for all subdomains, step counter 0 (CLbmSolver::reset). */
+int lbm_cu_domain_reset(lbm_domain *dom, void *stream);
+/* Seeded start-up keyed by physical cell (neighbours overlap by two cells). */
+int lbm_cu_domain_perturb(lbm_domain *dom, uint64_t seed, double amp, void *stream);
+/* `steps` calls of CController::computeNextStep for every subdomain
+ * (src/CController.hpp:385-391): one batched step launch over all
+ * subdomains, then the halo exchange in x, y, z order.  Whole pairs of steps
+ * replay a captured CUDA graph when use_graph != 0. */
+int lbm_cu_domain_run(lbm_domain *dom, int steps, int use_graph, void *stream);
+/* Velocity and density (when the domain stores them) are written on every
+ * `interval`-th step, like STORE_VELOCITY / STORE_DENSITY at interval 1
+ * (the default); interval 0 writes them only on the last step of each
+ * lbm_cu_domain_run call. */
+int lbm_cu_domain_set_store_interval(lbm_domain *dom, int interval);
+/* Time every step-kernel launch with a pair of CUDA events on the launching
+ * stream (steps then run without graph replay), and read the accumulated
+ * milliseconds and launch count (reset != 0 clears them).  Stands in for the
+ * reference's -DPROFILE event timestamps (src/libcl/CCL.hpp:1752-1776). */
+int lbm_cu_domain_profile(lbm_domain *dom, int enable);
+int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launches, int reset);
+int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
+int lbm_cu_domain_subdomains(const lbm_domain *dom, int *count, int sub_size[3]);
+lbm_lattice *lbm_cu_domain_lattice(lbm_domain *dom, int index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

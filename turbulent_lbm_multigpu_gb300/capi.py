@@ -1,0 +1,246 @@
+"""ctypes binding of liblbm_gb300.so -- the C ABI declared in include/lbm_gb300.h.
+
+The library must have been built for sm_103a (``build.build()``); there is no
+CPU fallback: loading fails loudly when the library is missing, and every
+call that fails raises ``LbmError`` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB
+
+F32, F64, F16, BF16 = 0, 1, 2, 3
+STORAGE_NAMES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16}
+FIELD_DD, FIELD_VELOCITY, FIELD_DENSITY, FIELD_FLAGS = 0, 1, 2, 3
+FLAG_OBSTACLE, FLAG_FLUID, FLAG_VELOCITY_INJECTION, FLAG_GHOST_LAYER = 1, 2, 4, 8
+
+
+class LbmError(RuntimeError):
+    pass
+
+
+class Params(C.Structure):
+    """lbm_params: kernel arguments in double (rounded to the arithmetic type by the library)."""
+
+    _fields_ = [("inv_tau", C.c_double), ("tau0", C.c_double), ("les_c", C.c_double),
+                ("gravity", C.c_double * 3), ("lid", C.c_double)]
+
+    @staticmethod
+    def make(inv_tau: float, tau0: float = 0.0, les_c: float = 0.0, gravity=(0.0, 0.0, 0.0), lid: float = 0.0):
+        p = Params()
+        p.inv_tau, p.tau0, p.les_c, p.lid = inv_tau, tau0, les_c, lid
+        for a in range(3):
+            p.gravity[a] = gravity[a]
+        return p
+
+
+def les_coefficient(cs: float) -> float:
+    """18*sqrt(2)*Cs^2 of the subgrid relaxation time."""
+    return 18.0 * math.sqrt(2.0) * cs * cs
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not Path(LIB).exists():
+        raise LbmError(f"{LIB} is not built: run `python -m turbulent_lbm_multigpu_gb300.build` "
+                       "(CUDA toolkit, sm_103a); there is no CPU fallback")
+    L = C.CDLL(str(LIB))
+    vp, ci, i64, u64, cd = C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_double
+    ip = C.POINTER(C.c_int)
+    sig = {
+        "lbm_cu_last_error": ([], C.c_char_p),
+        "lbm_cu_version": ([], C.c_char_p),
+        "lbm_cu_create": ([ci, ci, ci, ci, ci, ci, C.POINTER(vp)], ci),
+        "lbm_cu_destroy": ([vp], ci),
+        "lbm_cu_dims": ([vp, ip], ci),
+        "lbm_cu_set_params": ([vp, C.POINTER(Params)], ci),
+        "lbm_cu_init": ([vp, ip, vp], ci),
+        "lbm_cu_perturb": ([vp, ip, ip, u64, cd, vp], ci),
+        "lbm_cu_step": ([vp, ci, vp], ci),
+        "lbm_cu_read": ([vp, ci, ip, ip, vp, vp], ci),
+        "lbm_cu_write": ([vp, ci, ip, ip, vp, ip, vp], ci),
+        "lbm_cu_halo": ([vp, ip, vp, ip, ip, ip, vp], ci),
+        "lbm_cu_reduce_conserved": ([vp, ci, C.POINTER(cd), vp], ci),
+        "lbm_cu_domain_create": ([ip, ip, ci, ci, ci, ci, C.POINTER(vp)], ci),
+        "lbm_cu_domain_destroy": ([vp], ci),
+        "lbm_cu_domain_set_params": ([vp, C.POINTER(Params)], ci),
+        "lbm_cu_domain_reset": ([vp, vp], ci),
+        "lbm_cu_domain_perturb": ([vp, u64, cd, vp], ci),
+        "lbm_cu_domain_run": ([vp, ci, ci, vp], ci),
+        "lbm_cu_domain_counter": ([vp, C.POINTER(i64)], ci),
+        "lbm_cu_domain_set_store_interval": ([vp, ci], ci),
+        "lbm_cu_domain_profile": ([vp, ci], ci),
+        "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
+        "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
+        "lbm_cu_domain_lattice": ([vp, ci], vp),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != 0:
+        raise LbmError(lib().lbm_cu_last_error().decode())
+
+
+def ivec(v):
+    if v is None:
+        return None
+    return (C.c_int * len(v))(*[int(x) for x in v])
+
+
+def real_dtype(storage: int):
+    return np.float64 if storage == F64 else np.float32
+
+
+class Lattice:
+    """One lattice (subdomain) on the current GPU, owning its device fields."""
+
+    def __init__(self, nx, ny, nz, storage=F32, store_velocity=True, store_density=True, handle=None, owner=None):
+        self.dims = (int(nx), int(ny), int(nz))
+        self.storage = storage
+        self.store_velocity, self.store_density = bool(store_velocity), bool(store_density)
+        self._owner = owner
+        if handle is None:
+            h = C.c_void_p()
+            check(lib().lbm_cu_create(nx, ny, nz, storage, int(store_velocity), int(store_density), C.byref(h)))
+            self.h = h
+        else:
+            self.h = C.c_void_p(handle)
+
+    def close(self):
+        if self._owner is None and self.h:
+            lib().lbm_cu_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def cells(self):
+        return self.dims[0] * self.dims[1] * self.dims[2]
+
+    def set_params(self, p: Params):
+        check(lib().lbm_cu_set_params(self.h, C.byref(p)))
+
+    def init(self, bc, stream=None):
+        check(lib().lbm_cu_init(self.h, ivec(bc), stream))
+
+    def perturb(self, origin, phys, seed, amp, stream=None):
+        check(lib().lbm_cu_perturb(self.h, ivec(origin), ivec(phys), seed, amp, stream))
+
+    def step(self, parity: int, stream=None):
+        check(lib().lbm_cu_step(self.h, parity, stream))
+
+    def _shape(self, field, size):
+        sx, sy, sz = size
+        planes = {FIELD_DD: 19, FIELD_VELOCITY: 3, FIELD_DENSITY: 1, FIELD_FLAGS: 1}[field]
+        dt = np.int32 if field == FIELD_FLAGS else real_dtype(self.storage)
+        return (planes, sz, sy, sx), dt
+
+    def read(self, field, origin=None, size=None, out=None, stream=None):
+        size = tuple(size) if size is not None else self.dims
+        shape, dt = self._shape(field, size)
+        if out is None:
+            out = np.empty(shape, dt)
+        if out.dtype != dt or out.size != int(np.prod(shape)) or not out.flags.c_contiguous:
+            raise LbmError(f"host buffer must be a contiguous {dt.__name__} array of {int(np.prod(shape))} elements")
+        check(lib().lbm_cu_read(self.h, field, ivec(origin), ivec(size), out.ctypes.data_as(C.c_void_p), stream))
+        return out
+
+    def write(self, field, src, origin=None, size=None, norm=None, stream=None):
+        size = tuple(size) if size is not None else self.dims
+        shape, dt = self._shape(field, size)
+        src = np.ascontiguousarray(src, dtype=dt)
+        if src.size != int(np.prod(shape)):
+            raise LbmError(f"host buffer must hold {int(np.prod(shape))} elements")
+        check(lib().lbm_cu_write(self.h, field, ivec(origin), ivec(size), src.ctypes.data_as(C.c_void_p),
+                                 ivec(norm), stream))
+
+    def reduce_conserved(self, layout: int, stream=None):
+        out = (C.c_double * 5)()
+        check(lib().lbm_cu_reduce_conserved(self.h, layout, out, stream))
+        return np.array(out[:], dtype=np.float64)
+
+
+def halo(src: Lattice, src_origin, dst: Lattice, dst_origin, size, norm=None, stream=None):
+    check(lib().lbm_cu_halo(src.h, ivec(src_origin), dst.h, ivec(dst_origin), ivec(size), ivec(norm), stream))
+
+
+class Domain:
+    """A decomposed domain on one GPU (CManager + CController, device-local halos)."""
+
+    def __init__(self, size, nums, storage=F32, store_velocity=False, store_density=False, lid_geometry=True):
+        self.size, self.nums = tuple(size), tuple(nums)
+        self.storage = storage
+        h = C.c_void_p()
+        check(lib().lbm_cu_domain_create(ivec(size), ivec(nums), storage, int(store_velocity), int(store_density),
+                                         int(lid_geometry), C.byref(h)))
+        self.h = h
+        cnt = C.c_int()
+        sub = (C.c_int * 3)()
+        check(lib().lbm_cu_domain_subdomains(self.h, C.byref(cnt), sub))
+        self.sub = tuple(sub[:])
+        self.subdomains = [Lattice(*self.sub, storage, store_velocity, store_density,
+                                   handle=lib().lbm_cu_domain_lattice(self.h, i), owner=self) for i in range(cnt.value)]
+
+    def close(self):
+        if self.h:
+            lib().lbm_cu_domain_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def cells(self):
+        return self.size[0] * self.size[1] * self.size[2]
+
+    def set_params(self, p: Params):
+        check(lib().lbm_cu_domain_set_params(self.h, C.byref(p)))
+
+    def reset(self, stream=None):
+        check(lib().lbm_cu_domain_reset(self.h, stream))
+
+    def perturb(self, seed, amp, stream=None):
+        check(lib().lbm_cu_domain_perturb(self.h, seed, amp, stream))
+
+    def run(self, steps, use_graph=True, stream=None):
+        check(lib().lbm_cu_domain_run(self.h, steps, int(use_graph), stream))
+
+    @property
+    def counter(self):
+        c = C.c_int64()
+        check(lib().lbm_cu_domain_counter(self.h, C.byref(c)))
+        return c.value
+
+    def set_store_interval(self, interval: int):
+        check(lib().lbm_cu_domain_set_store_interval(self.h, interval))
+
+    def profile(self, enable: bool):
+        check(lib().lbm_cu_domain_profile(self.h, int(enable)))
+
+    def kernel_time(self, reset=False):
+        ms, n = C.c_double(), C.c_int64()
+        check(lib().lbm_cu_domain_kernel_time(self.h, C.byref(ms), C.byref(n), int(reset)))
+        return ms.value, n.value

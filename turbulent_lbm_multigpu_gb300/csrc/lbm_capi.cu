@@ -1,0 +1,1029 @@
+// lbm_capi.cu -- the C ABI of include/lbm_gb300.h over the sm_103a kernels.
+//
+// Host-side runtime: lattice handles own their device fields (like the
+// reference's CLbmSolver owns its CL buffers), parameters are rounded to the
+// arithmetic type once, and domains hold all subdomains of a decomposition on
+// one GPU with device-local halo copies and a captured CUDA graph per pair
+// of steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbm_gb300.h"
+#include "lbm_kernels.cuh"
+
+using namespace lbm;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(const std::string &m) {
+    g_err = m;
+    return -1;
+}
+
+#define CU(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) return fail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+constexpr int kBlock = 256;
+
+size_t storage_bytes(int st) { return st == kF64 ? 8 : st == kF32 ? 4 : 2; }
+size_t real_bytes(int st) { return st == kF64 ? 8 : 4; }
+
+int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+bool valid_box(const lbm_lattice *l, const int o[3], const int s[3]);
+}  // namespace
+
+struct lbm_lattice {
+    int nx, ny, nz;
+    int64_t n, pstride;
+    int storage;
+    int store_v, store_rho;
+    void *dd = nullptr;
+    uint8_t *flags = nullptr;
+    void *vel = nullptr;
+    void *rho = nullptr;
+    LatDesc h{};
+    LatDesc *d_desc = nullptr;
+    bool dirty = true;
+    void *stage = nullptr;  // staging for host copies and reduction partials
+    size_t stage_bytes = 0;
+};
+
+namespace {
+bool valid_box(const lbm_lattice *l, const int o[3], const int s[3]) {
+    const int d[3] = {l->nx, l->ny, l->nz};
+    for (int a = 0; a < 3; a++)
+        if (o[a] < 0 || s[a] < 0 || (int64_t)o[a] + s[a] > d[a]) return false;
+    return true;
+}
+
+int ensure_stage(lbm_lattice *l, size_t bytes) {
+    if (bytes <= l->stage_bytes) return 0;
+    if (l->stage) CU(cudaFree(l->stage));
+    l->stage = nullptr;
+    l->stage_bytes = 0;
+    CU(cudaMalloc(&l->stage, bytes));
+    l->stage_bytes = bytes;
+    return 0;
+}
+
+int upload_desc(lbm_lattice *l, cudaStream_t st) {
+    if (!l->dirty) return 0;
+    CU(cudaMemcpyAsync(l->d_desc, &l->h, sizeof(LatDesc), cudaMemcpyHostToDevice, st));
+    l->dirty = false;
+    return 0;
+}
+
+// Parameters rounded to the arithmetic type R, plus the gravity chain
+// coefficients of lbm_alpha.cl:183-291 computed in R.
+template <typename R> void fill_params(const lbm_params &p, R out[16], int *grav) {
+    const R gx = (R)p.gravity[0], gy = (R)p.gravity[1], gz = (R)p.gravity[2];
+    const R c18 = (R)(1.0f / 18.0f), c36 = (R)(1.0f / 36.0f);
+    out[P_INV_TAU] = (R)p.inv_tau;
+    out[P_TAU0] = (R)p.tau0;
+    out[P_LES] = (R)p.les_c;
+    out[P_LID] = (R)p.lid;
+    R k[9];
+    k[0] = gx * c18;
+    k[1] = gy * (R)(-1.0f / 18.0f);
+    k[2] = (gx - gy) * c36;
+    k[3] = (gx + gy) * c36;
+    k[4] = (gx + gz) * c36;
+    k[5] = (gx - gz) * c36;
+    k[6] = (gz - gy) * c36;
+    k[7] = (gz + gy) * (R)(-1.0f / 36.0f);
+    k[8] = gz * c18;
+    int any = 0;
+    for (int i = 0; i < 9; i++) {
+        out[P_K0 + i] = k[i];
+        if (k[i] != (R)0) any = 1;
+    }
+    *grav = any;
+}
+
+void set_params_desc(LatDesc &h, int storage, const lbm_params &p) {
+    int grav = 0;
+    if (storage == kF64) {
+        fill_params<double>(p, h.pd, &grav);
+        for (int i = 0; i < 16; i++) h.pf[i] = (float)h.pd[i];
+    } else {
+        fill_params<float>(p, h.pf, &grav);
+        for (int i = 0; i < 16; i++) h.pd[i] = (double)h.pf[i];
+    }
+    h.grav = grav;
+}
+
+bool uses_les(const LatDesc &h) { return h.pd[P_LES] != 0.0; }
+
+// ---------------------------------------------------------------- kernels
+template <typename S>
+__global__ void k_init(LatDesc d, int b0, int b1, int b2, int b3, int b4, int b5, int store_v, int store_rho) {
+    using R = typename Store<S>::R;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const int64_t x = c % d.nx, y = (c / d.nx) % d.ny, z = c / ((int64_t)d.nx * d.ny);
+    int fl = kFluid;  // x faces win over y faces, y over z (lbm_init.cl:53-68)
+    if (x == 0) fl = b0;
+    else if (x == d.nx - 1) fl = b1;
+    else if (y == 0) fl = b2;
+    else if (y == d.ny - 1) fl = b3;
+    else if (z == 0) fl = b4;
+    else if (z == d.nz - 1) fl = b5;
+    R eq[19];
+    const R dp = (R)1.0f - K<R>::k15 * ((R)0 * (R)0);
+    equilibria<R>((R)0, (R)0, (R)0, dp, eq);
+    S *dd = (S *)d.dd;
+#pragma unroll
+    for (int i = 0; i < 19; i++) Store<S>::st(dd + i * d.pstride + c, eq[i], weight<R>(i));
+    d.flags[c] = (uint8_t)fl;
+    if (store_v) {
+        R *u = (R *)d.vel;
+        u[c] = 0; u[d.n + c] = 0; u[2 * d.n + c] = 0;
+    }
+    if (store_rho) ((R *)d.rho)[c] = (R)1.0f;
+}
+
+// Philox4x32-10 (Salmon et al., SC'11), same as the oracle's.
+__device__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        const uint32_t n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        const uint32_t n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+template <typename S>
+__global__ void k_perturb(LatDesc d, int ox, int oy, int oz, int gx, int gy, int gz, uint64_t seed, double amp,
+                          int store_v, int store_rho) {
+    using R = typename Store<S>::R;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    const int64_t px = ox + c % d.nx, py = oy + (c / d.nx) % d.ny, pz = oz + c / ((int64_t)d.nx * d.ny);
+    if (px <= 0 || py <= 0 || pz <= 0 || px >= gx - 1 || py >= gy - 1 || pz >= gz - 1) return;
+    const uint64_t idx = (uint64_t)((pz * gy + py) * gx + px);
+    uint32_t r[4] = {(uint32_t)idx, (uint32_t)(idx >> 32), 0u, 0u};
+    philox(r, (uint32_t)seed, (uint32_t)(seed >> 32));
+    R u[3];
+    for (int a = 0; a < 3; a++) {
+        const double unit = (double)(r[a] >> 8) * (1.0 / 16777216.0);
+        u[a] = (R)((unit * 2.0 - 1.0) * amp);
+    }
+    const R v2 = (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2];
+    const R dp = (R)1.0f - K<R>::k15 * v2;
+    R eq[19];
+    equilibria<R>(u[0], u[1], u[2], dp, eq);
+    S *dd = (S *)d.dd;
+#pragma unroll
+    for (int i = 0; i < 19; i++) Store<S>::st(dd + opp(i) * d.pstride + c, eq[i], weight<R>(opp(i)));
+    if (store_v) {
+        R *v = (R *)d.vel;
+        v[c] = u[0]; v[d.n + c] = u[1]; v[2 * d.n + c] = u[2];
+    }
+    if (store_rho) ((R *)d.rho)[c] = (R)1.0f;
+}
+
+// Box copy between a lattice field and a packed [plane][z][y][x] buffer.
+struct Box {
+    int64_t lat_nx, lat_slice;   // lattice geometry
+    int ox, oy, oz, sx, sy, sz;  // rectangle
+    int64_t cells;               // sx*sy*sz
+    uint32_t mask;               // planes to copy
+    int nplanes;
+};
+
+__device__ __forceinline__ int64_t box_cell(const Box &b, int64_t k) {
+    const int64_t x = k % b.sx, y = (k / b.sx) % b.sy, z = k / ((int64_t)b.sx * b.sy);
+    return (b.oz + z) * b.lat_slice + (b.oy + y) * b.lat_nx + (b.ox + x);
+}
+
+// Populations: decode to the arithmetic type (pack) or encode (unpack).
+template <typename S, bool PACK>
+__global__ void k_box_dd(S *dd, int64_t pstride, typename Store<S>::R *buf, Box b) {
+    using R = typename Store<S>::R;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.cells * 19) return;
+    const int f = (int)(t / b.cells);
+    if (!((b.mask >> f) & 1u)) return;
+    const int64_t k = t - (int64_t)f * b.cells;
+    S *p = dd + f * pstride + box_cell(b, k);
+    R w = weight<R>(f);
+    if (PACK) buf[t] = Store<S>::ld(p, w);
+    else Store<S>::st(p, buf[t], w);
+}
+
+// Velocity / density planes: plain copies.
+template <typename R, bool PACK>
+__global__ void k_box_real(R *field, int64_t pstride, R *buf, Box b) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.cells * b.nplanes) return;
+    const int f = (int)(t / b.cells);
+    const int64_t k = t - (int64_t)f * b.cells;
+    R *p = field + f * pstride + box_cell(b, k);
+    if (PACK) buf[t] = *p;
+    else *p = buf[t];
+}
+
+template <bool PACK>
+__global__ void k_box_flags(uint8_t *flags, int32_t *buf, Box b) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.cells) return;
+    uint8_t *p = flags + box_cell(b, t);
+    if (PACK) buf[t] = *p;
+    else *p = (uint8_t)buf[t];
+}
+
+__global__ void k_check_flags(const int32_t *buf, int64_t cells, int *bad) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cells && (buf[t] < 0 || buf[t] > 255)) *bad = 1;
+}
+
+// Batched halo copies: every copy of one axis phase in one launch.
+struct HaloDesc {
+    void *src, *dst;
+    int64_t sps, dps;
+    Box sb, db;
+    int64_t first;  // first flat index of this copy
+};
+
+// One halo copy element: the j-th selected plane of cell k of the box.
+template <typename E>
+__device__ __forceinline__ void halo_elem(const HaloDesc &h, int64_t u) {
+    const int j = (int)(u / h.sb.cells);
+    const int64_t k = u - (int64_t)j * h.sb.cells;
+    uint32_t m = h.sb.mask;
+    for (int q = 0; q < j; q++) m &= m - 1;
+    const int f = __ffs(m) - 1;
+    ((E *)h.dst)[f * h.dps + box_cell(h.db, k)] = ((const E *)h.src)[f * h.sps + box_cell(h.sb, k)];
+}
+
+template <typename E>
+__global__ void k_halo_one(HaloDesc h, int64_t total) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < total) halo_elem<E>(h, t);
+}
+
+template <typename E>
+__global__ void k_halo_batch(const HaloDesc *__restrict__ hd, int nd, int64_t total) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (hd[mid].first <= t) lo = mid; else hi = mid - 1;
+    }
+    halo_elem<E>(hd[lo], t - hd[lo].first);
+}
+
+// Neumaier-compensated FP64 accumulation.
+struct Acc {
+    double s, c;
+    __device__ __forceinline__ void add(double v) {
+        const double t = s + v;
+        if (fabs(s) >= fabs(v)) c += (s - t) + v;
+        else c += (v - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ void merge(const Acc &o) {
+        add(o.s);
+        c += o.c;
+    }
+};
+
+constexpr int kRedBlocks = 1024;
+
+template <typename S>
+__global__ void __launch_bounds__(kBlock) k_reduce(LatDesc d, int layout, double *partial) {
+    using R = typename Store<S>::R;
+    __shared__ Acc sh[5][kBlock];
+    Acc a[5];
+    for (int q = 0; q < 5; q++) a[q] = Acc{0.0, 0.0};
+    const S *dd = (const S *)d.dd;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < d.n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (d.flags[c] != kFluid) continue;
+        double r = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+        for (int i = 0; i < 19; i++) {
+            const int slot = layout ? opp(i) : i;
+            const double f = (double)Store<S>::ld(dd + slot * d.pstride + c, weight<R>(slot));
+            r += f;
+            jx += dir_x(i) * f;
+            jy += dir_y(i) * f;
+            jz += dir_z(i) * f;
+        }
+        a[0].add(r);
+        a[1].add(jx);
+        a[2].add(jy);
+        a[3].add(jz);
+        a[4].add(0.5 * (jx * jx + jy * jy + jz * jz));
+    }
+    for (int q = 0; q < 5; q++) sh[q][threadIdx.x] = a[q];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int q = 0; q < 5; q++) sh[q][threadIdx.x].merge(sh[q][threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 5; q++) {
+            partial[(blockIdx.x * 5 + q) * 2] = sh[q][0].s;
+            partial[(blockIdx.x * 5 + q) * 2 + 1] = sh[q][0].c;
+        }
+}
+
+__global__ void k_reduce_final(const double *partial, int nblocks, double *out) {
+    if (threadIdx.x >= 5) return;
+    const int q = threadIdx.x;
+    Acc a{0.0, 0.0};
+    for (int b = 0; b < nblocks; b++) {
+        a.add(partial[(b * 5 + q) * 2]);
+        a.c += partial[(b * 5 + q) * 2 + 1];
+    }
+    out[q] = a.s + a.c;
+}
+
+// ------------------------------------------------------------- dispatchers
+template <typename S>
+int launch_step_t(int parity, bool les, const LatDesc *tab, int ntab, int blocks, int sv, int sr, cudaStream_t st) {
+    if (blocks <= 0) return 0;
+    if (parity) {
+        if (les) k_alpha<S, true><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+        else k_alpha<S, false><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+    } else {
+        if (les) k_beta<S, true><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+        else k_beta<S, false><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+    }
+    CU(cudaGetLastError());
+    return 0;
+}
+
+int launch_step(int storage, int parity, bool les, const LatDesc *tab, int ntab, int blocks, int sv, int sr,
+                cudaStream_t st) {
+    switch (storage) {
+        case kF32: return launch_step_t<float>(parity, les, tab, ntab, blocks, sv, sr, st);
+        case kF64: return launch_step_t<double>(parity, les, tab, ntab, blocks, sv, sr, st);
+        case kF16: return launch_step_t<__half>(parity, les, tab, ntab, blocks, sv, sr, st);
+        case kBF16: return launch_step_t<__nv_bfloat16>(parity, les, tab, ntab, blocks, sv, sr, st);
+    }
+    return fail("unknown storage type");
+}
+
+int grid_for(int64_t work) { return (int)((work + kBlock - 1) / kBlock); }
+
+Box make_box(const lbm_lattice *l, const int o[3], const int s[3], uint32_t mask) {
+    Box b;
+    b.lat_nx = l->nx;
+    b.lat_slice = (int64_t)l->nx * l->ny;
+    b.ox = o[0]; b.oy = o[1]; b.oz = o[2];
+    b.sx = s[0]; b.sy = s[1]; b.sz = s[2];
+    b.cells = (int64_t)s[0] * s[1] * s[2];
+    b.mask = mask;
+    b.nplanes = __builtin_popcount(mask);
+    return b;
+}
+
+uint32_t norm_mask(const int norm[3]) {
+    if (!norm) return (1u << 19) - 1;
+    uint32_t m = 0;
+    for (int f = 0; f < 19; f++)
+        if (norm[0] * dir_x(f) + norm[1] * dir_y(f) + norm[2] * dir_z(f) > 0) m |= 1u << f;
+    return m;
+}
+
+template <typename E>
+int launch_halo(const HaloDesc *d_hd, int nd, int64_t total, cudaStream_t st) {
+    if (total <= 0) return 0;
+    k_halo_batch<E><<<grid_for(total), kBlock, 0, st>>>(d_hd, nd, total);
+    CU(cudaGetLastError());
+    return 0;
+}
+
+template <typename E>
+int launch_halo_one(const HaloDesc &h, int64_t total, cudaStream_t st) {
+    k_halo_one<E><<<grid_for(total), kBlock, 0, st>>>(h, total);
+    CU(cudaGetLastError());
+    return 0;
+}
+
+int launch_halo_any(int storage, const HaloDesc *d_hd, int nd, int64_t total, cudaStream_t st) {
+    switch (storage_bytes(storage)) {
+        case 2: return launch_halo<uint16_t>(d_hd, nd, total, st);
+        case 4: return launch_halo<uint32_t>(d_hd, nd, total, st);
+        case 8: return launch_halo<uint64_t>(d_hd, nd, total, st);
+    }
+    return fail("bad storage size");
+}
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char *lbm_cu_last_error(void) { return g_err.c_str(); }
+
+const char *lbm_cu_version(void) {
+    return "lbm_gb300 D3Q19 A-A (alpha/beta), sm_103a, -fmad=false, IEEE div/sqrt";
+}
+
+int lbm_cu_create(int nx, int ny, int nz, int storage, int store_velocity, int store_density, lbm_lattice **out) {
+    if (!out) return fail("out is NULL");
+    *out = nullptr;
+    if (nx < 3 || ny < 3 || nz < 3) return fail("each lattice dimension must be at least 3");
+    if (storage < kF32 || storage > kBF16) return fail("unknown storage type");
+    const int64_t n = (int64_t)nx * ny * nz;
+    if (n > ((int64_t)1 << 31) - 1) return fail("lattice has more than 2^31-1 cells");
+    lbm_lattice *l = new lbm_lattice();
+    l->nx = nx; l->ny = ny; l->nz = nz;
+    l->n = n;
+    l->pstride = round_up(n, 256 / (int64_t)storage_bytes(storage));
+    l->storage = storage;
+    l->store_v = store_velocity ? 1 : 0;
+    l->store_rho = store_density ? 1 : 0;
+    auto cleanup = [&](const std::string &m) {
+        lbm_cu_destroy(l);
+        return fail(m);
+    };
+    if (cudaMalloc(&l->dd, (size_t)l->pstride * 19 * storage_bytes(storage)) != cudaSuccess)
+        return cleanup("cudaMalloc of the population planes failed");
+    if (cudaMalloc((void **)&l->flags, (size_t)round_up(n, 256)) != cudaSuccess) return cleanup("cudaMalloc of flags failed");
+    if (l->store_v && cudaMalloc(&l->vel, (size_t)n * 3 * real_bytes(storage)) != cudaSuccess)
+        return cleanup("cudaMalloc of velocity failed");
+    if (l->store_rho && cudaMalloc(&l->rho, (size_t)n * real_bytes(storage)) != cudaSuccess)
+        return cleanup("cudaMalloc of density failed");
+    if (cudaMalloc((void **)&l->d_desc, sizeof(LatDesc)) != cudaSuccess) return cleanup("cudaMalloc of descriptor failed");
+    LatDesc &h = l->h;
+    h.dd = l->dd; h.flags = l->flags; h.vel = l->vel; h.rho = l->rho;
+    h.pstride = l->pstride; h.n = n;
+    h.nx = nx; h.ny = ny; h.nz = nz;
+    h.first_block = 0;
+    h.nblocks = grid_for(n);
+    lbm_params p{};
+    p.inv_tau = 1.0 / 0.953575;  // reference default tau (src/CLbmSkeleton.hpp:142)
+    p.tau0 = 0.953575;
+    set_params_desc(h, storage, p);
+    l->dirty = true;
+    cudaGetLastError();
+    *out = l;
+    return 0;
+}
+
+int lbm_cu_destroy(lbm_lattice *l) {
+    if (!l) return 0;
+    if (l->dd) cudaFree(l->dd);
+    if (l->flags) cudaFree(l->flags);
+    if (l->vel) cudaFree(l->vel);
+    if (l->rho) cudaFree(l->rho);
+    if (l->d_desc) cudaFree(l->d_desc);
+    if (l->stage) cudaFree(l->stage);
+    delete l;
+    return 0;
+}
+
+int lbm_cu_dims(const lbm_lattice *l, int dims[3]) {
+    if (!l || !dims) return fail("NULL argument");
+    dims[0] = l->nx; dims[1] = l->ny; dims[2] = l->nz;
+    return 0;
+}
+
+int lbm_cu_set_params(lbm_lattice *l, const lbm_params *p) {
+    if (!l || !p) return fail("NULL argument");
+    if (p->les_c != 0.0 && !(p->tau0 > 0.5)) return fail("the subgrid model needs tau0 > 0.5");
+    set_params_desc(l->h, l->storage, *p);
+    l->dirty = true;
+    return 0;
+}
+
+int lbm_cu_init(lbm_lattice *l, const int bc[6], void *stream) {
+    if (!l || !bc) return fail("NULL argument");
+    for (int i = 0; i < 6; i++)
+        if (bc[i] < 0 || bc[i] > 255) return fail("boundary flags must fit in one byte");
+    const int g = grid_for(l->n);
+    switch (l->storage) {
+        case kF32: k_init<float><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
+        case kF64: k_init<double><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
+        case kF16: k_init<__half><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
+        case kBF16: k_init<__nv_bfloat16><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
+    }
+    CU(cudaGetLastError());
+    return 0;
+}
+
+int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t seed, double amp, void *stream) {
+    if (!l || !o || !ph) return fail("NULL argument");
+    const int g = grid_for(l->n);
+#define PERT(S_) k_perturb<S_><<<g, kBlock, 0, S(stream)>>>(l->h, o[0], o[1], o[2], ph[0], ph[1], ph[2], seed, amp, l->store_v, l->store_rho)
+    switch (l->storage) {
+        case kF32: PERT(float); break;
+        case kF64: PERT(double); break;
+        case kF16: PERT(__half); break;
+        case kBF16: PERT(__nv_bfloat16); break;
+    }
+#undef PERT
+    CU(cudaGetLastError());
+    return 0;
+}
+
+int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
+    if (!l) return fail("NULL lattice");
+    if (upload_desc(l, S(stream))) return -1;
+    return launch_step(l->storage, parity & 1, uses_les(l->h), l->d_desc, 1, l->h.nblocks, l->store_v, l->store_rho,
+                       S(stream));
+}
+
+static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], void *host, const int norm[3],
+                  bool read, cudaStream_t st) {
+    static const int zero[3] = {0, 0, 0};
+    int full[3] = {l->nx, l->ny, l->nz};
+    if (!o) o = zero;
+    if (!s) s = full;
+    if (!valid_box(l, o, s)) return fail("rectangle outside the lattice");
+    if (!host) return fail("NULL host buffer");
+    const int64_t cells = (int64_t)s[0] * s[1] * s[2];
+    if (cells == 0) return 0;
+    const size_t rb = real_bytes(l->storage);
+    int nplanes;
+    size_t ebytes;
+    switch (field) {
+        case LBM_FIELD_DD: nplanes = 19; ebytes = rb; break;
+        case LBM_FIELD_VELOCITY:
+            if (!l->vel) return fail("velocity is not stored by this lattice");
+            nplanes = 3; ebytes = rb; break;
+        case LBM_FIELD_DENSITY:
+            if (!l->rho) return fail("density is not stored by this lattice");
+            nplanes = 1; ebytes = rb; break;
+        case LBM_FIELD_FLAGS: nplanes = 1; ebytes = 4; break;
+        default: return fail("unknown field");
+    }
+    const size_t bytes = (size_t)cells * nplanes * ebytes;
+    if (ensure_stage(l, bytes + 256)) return -1;
+    const uint32_t mask = field == LBM_FIELD_DD ? norm_mask(read ? nullptr : norm) : (1u << nplanes) - 1;
+    Box b = make_box(l, o, s, mask);
+    if (!read) CU(cudaMemcpyAsync(l->stage, host, bytes, cudaMemcpyHostToDevice, st));
+    const int g = grid_for(cells * nplanes);
+    if (field == LBM_FIELD_DD) {
+#define BOX(S_, R_)                                                                                          \
+    (read ? k_box_dd<S_, true><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b)             \
+          : k_box_dd<S_, false><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b))
+        switch (l->storage) {
+            case kF32: BOX(float, float); break;
+            case kF64: BOX(double, double); break;
+            case kF16: BOX(__half, float); break;
+            case kBF16: BOX(__nv_bfloat16, float); break;
+        }
+#undef BOX
+    } else if (field == LBM_FIELD_FLAGS) {
+        if (!read) {
+            int *bad = (int *)((char *)l->stage + bytes);
+            CU(cudaMemsetAsync(bad, 0, sizeof(int), st));
+            k_check_flags<<<grid_for(cells), kBlock, 0, st>>>((const int32_t *)l->stage, cells, bad);
+            int hbad = 0;
+            CU(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            if (hbad) return fail("flag values must lie in [0, 255]");
+            k_box_flags<false><<<g, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
+        } else {
+            k_box_flags<true><<<g, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
+        }
+    } else {
+        void *fieldp = field == LBM_FIELD_VELOCITY ? l->vel : l->rho;
+        if (rb == 8) {
+            if (read) k_box_real<double, true><<<g, kBlock, 0, st>>>((double *)fieldp, l->n, (double *)l->stage, b);
+            else k_box_real<double, false><<<g, kBlock, 0, st>>>((double *)fieldp, l->n, (double *)l->stage, b);
+        } else {
+            if (read) k_box_real<float, true><<<g, kBlock, 0, st>>>((float *)fieldp, l->n, (float *)l->stage, b);
+            else k_box_real<float, false><<<g, kBlock, 0, st>>>((float *)fieldp, l->n, (float *)l->stage, b);
+        }
+    }
+    CU(cudaGetLastError());
+    if (read) CU(cudaMemcpyAsync(host, l->stage, bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int lbm_cu_read(lbm_lattice *l, int field, const int origin[3], const int size[3], void *host_dst, void *stream) {
+    if (!l) return fail("NULL lattice");
+    return box_io(l, field, origin, size, host_dst, nullptr, true, S(stream));
+}
+
+int lbm_cu_write(lbm_lattice *l, int field, const int origin[3], const int size[3], const void *host_src,
+                 const int norm[3], void *stream) {
+    if (!l) return fail("NULL lattice");
+    if (norm && field != LBM_FIELD_DD) return fail("a normal mask applies to populations only");
+    return box_io(l, field, origin, size, const_cast<void *>(host_src), norm, false, S(stream));
+}
+
+int lbm_cu_halo(lbm_lattice *src, const int so[3], lbm_lattice *dst, const int dof[3], const int size[3],
+                const int norm[3], void *stream) {
+    if (!src || !dst || !so || !dof || !size) return fail("NULL argument");
+    if (src->storage != dst->storage) return fail("halo copy between lattices of different storage");
+    if (!valid_box(src, so, size) || !valid_box(dst, dof, size)) return fail("halo rectangle outside a lattice");
+    const uint32_t mask = norm_mask(norm);
+    HaloDesc h;
+    h.src = src->dd; h.dst = dst->dd;
+    h.sps = src->pstride; h.dps = dst->pstride;
+    h.sb = make_box(src, so, size, mask);
+    h.db = make_box(dst, dof, size, mask);
+    h.first = 0;
+    const int64_t total = h.sb.cells * h.sb.nplanes;
+    if (total == 0) return 0;
+    switch (storage_bytes(src->storage)) {
+        case 2: return launch_halo_one<uint16_t>(h, total, S(stream));
+        case 4: return launch_halo_one<uint32_t>(h, total, S(stream));
+        default: return launch_halo_one<uint64_t>(h, total, S(stream));
+    }
+}
+
+int lbm_cu_reduce_conserved(lbm_lattice *l, int layout, double out[5], void *stream) {
+    if (!l || !out) return fail("NULL argument");
+    const size_t need = (size_t)kRedBlocks * 10 * sizeof(double) + 8 * sizeof(double);
+    if (ensure_stage(l, need)) return -1;
+    double *partial = (double *)l->stage;
+    double *res = partial + (size_t)kRedBlocks * 10;
+    const int blocks = std::min<int64_t>(kRedBlocks, std::max<int64_t>(1, grid_for(l->n)));
+    cudaStream_t st = S(stream);
+    switch (l->storage) {
+        case kF32: k_reduce<float><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kF64: k_reduce<double><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kF16: k_reduce<__half><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kBF16: k_reduce<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+    }
+    CU(cudaGetLastError());
+    k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, res);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return 0;
+}
+
+}  // extern "C"
+
+// ================================================================== domain
+struct CommGeom {
+    int dst;
+    int axis;
+    int send_origin[3], recv_origin[3], size[3], dir[3];
+};
+
+struct lbm_domain {
+    int size[3], nums[3], sub[3];
+    int storage, store_v, store_rho, lid_geometry;
+    std::vector<lbm_lattice *> subs;
+    std::vector<std::vector<CommGeom>> comms;
+    std::vector<std::vector<int>> bc;
+    std::vector<int> coords;  // 3 per subdomain
+    LatDesc *d_tab = nullptr;
+    int blocks = 0;
+    bool tab_dirty = true;
+    // halo plans [0 = after beta, 1 = after alpha][axis]
+    std::vector<HaloDesc> plan[2][3];
+    HaloDesc *d_plan[2][3] = {};
+    int64_t plan_total[2][3] = {};
+    int64_t counter = 0;
+    int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    // step-kernel timing with CUDA events (eager steps only)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;  // pairs: start, stop
+    size_t ev_used = 0;
+    double kernel_ms = 0.0;
+    int64_t kernel_launches = 0;
+};
+
+namespace {
+int domain_build_plans(lbm_domain *D) {
+    for (int ph = 0; ph < 2; ph++)
+        for (int a = 0; a < 3; a++) {
+            auto &v = D->plan[ph][a];
+            v.clear();
+            int64_t first = 0;
+            for (size_t b = 0; b < D->subs.size(); b++) {
+                for (const CommGeom &cm : D->comms[b]) {
+                    if (cm.axis != a) continue;
+                    // neighbour's comm pointing back at b
+                    const CommGeom *back = nullptr;
+                    for (const CommGeom &o : D->comms[cm.dst])
+                        if (o.dst == (int)b && o.axis == a) back = &o;
+                    if (!back) return fail("inconsistent CComm geometry");
+                    lbm_lattice *A = D->subs[cm.dst], *B = D->subs[b];
+                    HaloDesc h;
+                    h.src = A->dd; h.dst = B->dd;
+                    h.sps = A->pstride; h.dps = B->pstride;
+                    if (ph == 1) {  // syncAlpha: neighbour's inner layer -> own ghost layer, 19 planes
+                        h.sb = make_box(A, back->send_origin, back->size, (1u << 19) - 1);
+                        h.db = make_box(B, cm.recv_origin, cm.size, (1u << 19) - 1);
+                    } else {        // syncBeta: neighbour's ghost layer -> own inner layer, inward planes
+                        const uint32_t m = norm_mask(cm.dir);
+                        h.sb = make_box(A, back->recv_origin, back->size, m);
+                        h.db = make_box(B, cm.send_origin, cm.size, m);
+                    }
+                    h.first = first;
+                    first += h.sb.cells * h.sb.nplanes;
+                    v.push_back(h);
+                }
+            }
+            D->plan_total[ph][a] = first;
+            if (D->d_plan[ph][a]) {
+                cudaFree(D->d_plan[ph][a]);
+                D->d_plan[ph][a] = nullptr;
+            }
+            if (!v.empty()) {
+                CU(cudaMalloc((void **)&D->d_plan[ph][a], v.size() * sizeof(HaloDesc)));
+                CU(cudaMemcpy(D->d_plan[ph][a], v.data(), v.size() * sizeof(HaloDesc), cudaMemcpyHostToDevice));
+            }
+        }
+    return 0;
+}
+
+int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
+    if (!D->tab_dirty) return 0;
+    std::vector<LatDesc> tab;
+    int first = 0;
+    for (auto *l : D->subs) {
+        LatDesc h = l->h;
+        h.first_block = first;
+        first += h.nblocks;
+        tab.push_back(h);
+    }
+    D->blocks = first;
+    CU(cudaMemcpyAsync(D->d_tab, tab.data(), tab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice, st));
+    CU(cudaStreamSynchronize(st));
+    D->tab_dirty = false;
+    return 0;
+}
+
+int domain_record(lbm_domain *D, cudaStream_t st, cudaEvent_t *out) {
+    if (D->ev_used == D->ev.size()) {
+        cudaEvent_t e;
+        CU(cudaEventCreate(&e));
+        D->ev.push_back(e);
+    }
+    *out = D->ev[D->ev_used++];
+    CU(cudaEventRecord(*out, st));
+    return 0;
+}
+
+int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool timed) {
+    const bool les = uses_les(D->subs[0]->h);
+    const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (timed && domain_record(D, st, &e0)) return -1;
+    if (launch_step(D->storage, parity, les, D->d_tab, (int)D->subs.size(), D->blocks, sv, sr, st)) return -1;
+    if (timed && domain_record(D, st, &e1)) return -1;
+    for (int a = 0; a < 3; a++)
+        if (D->plan_total[parity][a] > 0 &&
+            launch_halo_any(D->storage, D->d_plan[parity][a], (int)D->plan[parity][a].size(), D->plan_total[parity][a], st))
+            return -1;
+    return 0;
+}
+
+void drop_graph(lbm_domain *D) {
+    if (D->graph) cudaGraphExecDestroy(D->graph);
+    D->graph = nullptr;
+}
+}  // namespace
+
+extern "C" {
+
+int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int store_velocity, int store_density,
+                         int lid_geometry, lbm_domain **out) {
+    if (!size || !nums || !out) return fail("NULL argument");
+    *out = nullptr;
+    for (int a = 0; a < 3; a++) {
+        if (nums[a] < 1 || size[a] < 1) return fail("sizes and subdomain counts must be positive");
+        if (size[a] % nums[a] != 0) return fail("Number of subdomains does not match with the grid size!");
+    }
+    lbm_domain *D = new lbm_domain();
+    for (int a = 0; a < 3; a++) {
+        D->size[a] = size[a];
+        D->nums[a] = nums[a];
+        D->sub[a] = size[a] / nums[a];
+    }
+    D->storage = storage;
+    D->store_v = store_velocity ? 1 : 0;
+    D->store_rho = store_density ? 1 : 0;
+    D->lid_geometry = lid_geometry;
+    const int nsub = nums[0] * nums[1] * nums[2];
+    const int stride[3] = {1, nums[0], nums[0] * nums[1]};
+    for (int id = 0; id < nsub; id++) {
+        lbm_lattice *l = nullptr;
+        if (lbm_cu_create(D->sub[0], D->sub[1], D->sub[2], storage, store_velocity, store_density, &l)) {
+            std::string m = g_err;
+            lbm_cu_domain_destroy(D);
+            return fail(m);
+        }
+        D->subs.push_back(l);
+        const int c[3] = {id % nums[0], (id / nums[0]) % nums[1], id / (nums[0] * nums[1])};
+        D->coords.insert(D->coords.end(), c, c + 3);
+        std::vector<int> bc(6, LBM_FLAG_GHOST_LAYER);
+        for (int a = 0; a < 3; a++) {
+            if (c[a] == 0) bc[2 * a] = LBM_FLAG_OBSTACLE;
+            if (c[a] == nums[a] - 1) bc[2 * a + 1] = LBM_FLAG_OBSTACLE;
+        }
+        std::vector<CommGeom> cms;
+        for (int a = 0; a < 3; a++)
+            for (int up = 0; up < 2; up++) {
+                if (bc[2 * a + up] != LBM_FLAG_GHOST_LAYER) continue;
+                CommGeom g{};
+                g.dst = id + (up ? stride[a] : -stride[a]);
+                g.axis = a;
+                for (int q = 0; q < 3; q++) {
+                    g.size[q] = q == a ? 1 : D->sub[q];
+                    g.send_origin[q] = g.recv_origin[q] = g.dir[q] = 0;
+                }
+                g.send_origin[a] = up ? D->sub[a] - 2 : 1;
+                g.recv_origin[a] = up ? D->sub[a] - 1 : 0;
+                g.dir[a] = up ? -1 : 1;
+                cms.push_back(g);
+            }
+        D->bc.push_back(bc);
+        D->comms.push_back(cms);
+    }
+    if (cudaMalloc((void **)&D->d_tab, nsub * sizeof(LatDesc)) != cudaSuccess) {
+        lbm_cu_domain_destroy(D);
+        return fail("cudaMalloc of the subdomain table failed");
+    }
+    if (domain_build_plans(D)) {
+        std::string m = g_err;
+        lbm_cu_domain_destroy(D);
+        return fail(m);
+    }
+    *out = D;
+    return 0;
+}
+
+int lbm_cu_domain_destroy(lbm_domain *D) {
+    if (!D) return 0;
+    drop_graph(D);
+    if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
+    for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
+    for (auto *l : D->subs) lbm_cu_destroy(l);
+    if (D->d_tab) cudaFree(D->d_tab);
+    for (int p = 0; p < 2; p++)
+        for (int a = 0; a < 3; a++)
+            if (D->d_plan[p][a]) cudaFree(D->d_plan[p][a]);
+    delete D;
+    return 0;
+}
+
+int lbm_cu_domain_set_params(lbm_domain *D, const lbm_params *p) {
+    if (!D || !p) return fail("NULL argument");
+    for (auto *l : D->subs)
+        if (lbm_cu_set_params(l, p)) return -1;
+    D->tab_dirty = true;
+    drop_graph(D);
+    return 0;
+}
+
+int lbm_cu_domain_reset(lbm_domain *D, void *stream) {
+    if (!D) return fail("NULL domain");
+    for (size_t i = 0; i < D->subs.size(); i++) {
+        lbm_lattice *l = D->subs[i];
+        if (lbm_cu_init(l, D->bc[i].data(), stream)) return -1;
+        if (D->lid_geometry && D->coords[3 * i + 1] == D->nums[1] - 1) {
+            // CController::setGeometry: lid plane y = Y-2, x in [1,X-2], z in [1,Z-2]
+            const int o[3] = {1, l->ny - 2, 1};
+            const int s[3] = {l->nx - 2, 1, l->nz - 2};
+            std::vector<int32_t> v((size_t)s[0] * s[1] * s[2], LBM_FLAG_VELOCITY_INJECTION);
+            if (lbm_cu_write(l, LBM_FIELD_FLAGS, o, s, v.data(), nullptr, stream)) return -1;
+        }
+    }
+    D->counter = 0;
+    return 0;
+}
+
+int lbm_cu_domain_perturb(lbm_domain *D, uint64_t seed, double amp, void *stream) {
+    if (!D) return fail("NULL domain");
+    int ph[3];
+    for (int a = 0; a < 3; a++) ph[a] = D->nums[a] * (D->sub[a] - 2) + 2;
+    for (size_t i = 0; i < D->subs.size(); i++) {
+        int o[3];
+        for (int a = 0; a < 3; a++) o[a] = D->coords[3 * i + a] * (D->sub[a] - 2);
+        if (lbm_cu_perturb(D->subs[i], o, ph, seed, amp, stream)) return -1;
+    }
+    return 0;
+}
+
+int lbm_cu_domain_run(lbm_domain *D, int steps, int use_graph, void *stream) {
+    if (!D) return fail("NULL domain");
+    if (steps < 0) return fail("negative step count");
+    cudaStream_t st = S(stream);
+    if (domain_upload_tab(D, st)) return -1;
+    int done = 0;
+    // u/rho are written on steps whose new counter is a multiple of the
+    // interval, or (interval 0) on the last step of this call
+    auto stores_on = [&](int64_t next_counter, bool last) {
+        return D->store_interval == 0 ? last : (next_counter % D->store_interval) == 0;
+    };
+    auto single = [&]() -> int {
+        const bool last = done + 1 == steps;
+        if (domain_one_step(D, (int)(D->counter & 1), st, stores_on(D->counter + 1, last), D->profile)) return -1;
+        D->counter++;
+        done++;
+        return 0;
+    };
+    if ((D->counter & 1) && done < steps)
+        if (single()) return -1;
+    // graph replay only where no pair needs a store or a timing record
+    const bool plain_pairs = (D->store_interval == 0) || (!D->store_v && !D->store_rho);
+    int pairs = (steps - done) / 2;
+    if (D->store_interval == 0 && (steps - done) % 2 == 0 && pairs > 0) pairs--;  // last pair stores
+    if (pairs > 0 && use_graph && plain_pairs && !D->profile) {
+        if (!D->graph) {
+            if (!D->cap_stream) CU(cudaStreamCreateWithFlags(&D->cap_stream, cudaStreamNonBlocking));
+            cudaGraph_t g = nullptr;
+            CU(cudaStreamBeginCapture(D->cap_stream, cudaStreamCaptureModeThreadLocal));
+            int rc = domain_one_step(D, 0, D->cap_stream, false, false);
+            if (!rc) rc = domain_one_step(D, 1, D->cap_stream, false, false);
+            cudaError_t e = cudaStreamEndCapture(D->cap_stream, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return -1;
+            }
+            if (e != cudaSuccess) return fail(std::string("graph capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&D->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                D->graph = nullptr;
+                return fail(std::string("graph instantiate: ") + cudaGetErrorString(e));
+            }
+        }
+        for (int p = 0; p < pairs; p++) CU(cudaGraphLaunch(D->graph, st));
+        D->counter += 2 * pairs;
+        done += 2 * pairs;
+    }
+    while (done < steps)
+        if (single()) return -1;
+    return 0;
+}
+
+int lbm_cu_domain_set_store_interval(lbm_domain *D, int interval) {
+    if (!D) return fail("NULL domain");
+    if (interval < 0) return fail("negative store interval");
+    D->store_interval = interval;
+    return 0;
+}
+
+int lbm_cu_domain_profile(lbm_domain *D, int enable) {
+    if (!D) return fail("NULL domain");
+    D->profile = enable != 0;
+    return 0;
+}
+
+int lbm_cu_domain_kernel_time(lbm_domain *D, double *ms_total, int64_t *launches, int reset) {
+    if (!D) return fail("NULL domain");
+    for (size_t i = 0; i + 1 < D->ev_used; i += 2) {
+        CU(cudaEventSynchronize(D->ev[i + 1]));
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, D->ev[i], D->ev[i + 1]));
+        D->kernel_ms += ms;
+        D->kernel_launches++;
+    }
+    D->ev_used = 0;
+    if (ms_total) *ms_total = D->kernel_ms;
+    if (launches) *launches = D->kernel_launches;
+    if (reset) {
+        D->kernel_ms = 0.0;
+        D->kernel_launches = 0;
+    }
+    return 0;
+}
+
+int lbm_cu_domain_counter(const lbm_domain *D, int64_t *counter) {
+    if (!D || !counter) return fail("NULL argument");
+    *counter = D->counter;
+    return 0;
+}
+
+int lbm_cu_domain_subdomains(const lbm_domain *D, int *count, int sub_size[3]) {
+    if (!D) return fail("NULL domain");
+    if (count) *count = (int)D->subs.size();
+    if (sub_size)
+        for (int a = 0; a < 3; a++) sub_size[a] = D->sub[a];
+    return 0;
+}
+
+lbm_lattice *lbm_cu_domain_lattice(lbm_domain *D, int index) {
+    if (!D || index < 0 || index >= (int)D->subs.size()) {
+        fail("subdomain index out of range");
+        return nullptr;
+    }
+    return D->subs[index];
+}
+
+}  // extern "C"
