@@ -70,6 +70,24 @@ def init_dist(ws, backend):
     return None
 
 
+def max_over_ranks(ms: float, dist) -> float:
+    """The slowest rank's time (the whole job ends with it)."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mlups(cells: int, steps: int, ms: float, world: int) -> float:
+    """Cell updates of all ranks (independent replicas) per second, in millions."""
+    return cells * steps * world / (ms * 1e-3) / 1e6
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -161,9 +179,10 @@ def cpu_run(cells_z: int, steps: int, warmup: int, threads: int):
     return cells * steps / dt / 1e6, dt, cells
 
 
-def cpu_baseline_sample():
+def cpu_baseline_sample(target_s=12.0):
     threads = os.cpu_count() or 1
-    z = 16
+    m0, _, _ = cpu_run(8, 2, 1, threads)
+    z = int(max(8, min(SIZE[2], target_s * m0 * 1e6 / (4 * SIZE[0] * SIZE[1]))))
     mlups, dt, cells = cpu_run(z, 4, 1, threads)
     return {"value": round(mlups, 2), "unit": "MLUPS", "cores": threads, "kind": "port",
             "sample": f"oracle port (C, OpenMP) of the reference kernels, 256x256x{z} slab of the same "
@@ -220,7 +239,7 @@ def run_gpu(args):
     pp = lattice_params(np.float32)
     prm = api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
 
-    D = api.Domain(SIZE, NUMS, api.F32, store_velocity=False, store_density=False)
+    D = api.Domain(args.size, args.nums, api.F32, store_velocity=False, store_density=False)
     D.set_params(prm)
     D.reset()
     D.perturb(SEED, AMP)
@@ -244,12 +263,11 @@ def run_gpu(args):
     ms = start.elapsed_time(stop)
     k_ms, k_n = D.kernel_time(reset=True)
     D.profile(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     cells = D.cells
-    mlups = cells * args.steps * ws / (ms * 1e-3) / 1e6
+    mlups = whole_job_mlups(cells, args.steps, ms, ws)
+    if args.steps < 2:
+        raise SystemExit("need at least 2 timed steps")
 
     # the same with CUDA-graph replay of step pairs
     torch.cuda.synchronize()
@@ -274,13 +292,14 @@ def run_gpu(args):
     del D
 
     # e2e through the C ABI with host buffers
-    e2e = run_e2e(api, prm, args.steps)
+    e2e = None if args.no_e2e else run_e2e(api, prm, args.steps)
 
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config_dict(), "roofline": roofline, "e2e": e2e,
+        "config": config_dict(None if tuple(args.size) == SIZE else f"profiling size {args.size}"),
+        "roofline": roofline, "e2e": e2e,
         "gpu_launches": int(args.steps * (1 + 2)),
         "clocks": clk.summary(),
         "graph_mlups": round(graph_mlups, 1),
@@ -344,6 +363,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
+    ap.add_argument("--size", type=int, nargs=3, default=list(SIZE), help="domain size (profiling only)")
+    ap.add_argument("--nums", type=int, nargs=3, default=list(NUMS), help="subdomains (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

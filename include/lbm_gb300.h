@@ -63,6 +63,10 @@ const char *lbm_cu_last_error(void);
 /* Library build string (kernels, architecture, compile options). */
 const char *lbm_cu_version(void);
 
+/* Wait for all work on `stream` (NULL: the whole device).  Replaces
+ * CLbmSolver::wait / clFinish (src/CLbmSolver.hpp:681-683). */
+int lbm_cu_synchronize(void *stream);
+
 /* ---------------------------------------------------------------- lattice */
 
 /* Allocate the fields of one nx*ny*nz lattice on the current device.

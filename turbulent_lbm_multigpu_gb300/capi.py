@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
     sig = {
         "lbm_cu_last_error": ([], C.c_char_p),
         "lbm_cu_version": ([], C.c_char_p),
+        "lbm_cu_synchronize": ([vp], ci),
         "lbm_cu_create": ([ci, ci, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_destroy": ([vp], ci),
         "lbm_cu_dims": ([vp, ip], ci),

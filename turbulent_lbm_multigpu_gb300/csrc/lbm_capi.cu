@@ -440,6 +440,12 @@ const char *lbm_cu_version(void) {
     return "lbm_gb300 D3Q19 A-A (alpha/beta), sm_103a, -fmad=false, IEEE div/sqrt";
 }
 
+int lbm_cu_synchronize(void *stream) {
+    if (stream) CU(cudaStreamSynchronize(S(stream)));
+    else CU(cudaDeviceSynchronize());
+    return 0;
+}
+
 int lbm_cu_create(int nx, int ny, int nz, int storage, int store_velocity, int store_density, lbm_lattice **out) {
     if (!out) return fail("out is NULL");
     *out = nullptr;
