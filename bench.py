@@ -43,6 +43,7 @@ SIZE = (256, 256, 256)
 NUMS = (2, 2, 1)
 U_LID, RE, CS, SEED, AMP = 0.1, 10000.0, 0.17, 1234, 1e-3
 BYTES_PER_CELL = {"f32": 152, "f64": 304, "f16": 76, "bf16": 76}
+HALO_MODE = 1  # after alpha, exchange the 5 populations the ghost layer's inner neighbours read
 
 
 def lattice_params(dtype):
@@ -180,13 +181,15 @@ def cpu_run(cells_z: int, steps: int, warmup: int, threads: int):
 
 
 def cpu_baseline_sample(target_s=12.0):
+    """Full 256^3 domain, as many timed steps as fit in about target_s seconds."""
     threads = os.cpu_count() or 1
-    m0, _, _ = cpu_run(8, 2, 1, threads)
-    z = int(max(8, min(SIZE[2], target_s * m0 * 1e6 / (4 * SIZE[0] * SIZE[1]))))
-    mlups, dt, cells = cpu_run(z, 4, 1, threads)
+    m0, _, _ = cpu_run(SIZE[2], 1, 1, threads)
+    steps = int(max(2, min(200, target_s * m0 * 1e6 / (SIZE[0] * SIZE[1] * SIZE[2]))))
+    z = SIZE[2]
+    mlups, dt, cells = cpu_run(z, steps, 0, threads)
     return {"value": round(mlups, 2), "unit": "MLUPS", "cores": threads, "kind": "port",
-            "sample": f"oracle port (C, OpenMP) of the reference kernels, 256x256x{z} slab of the same "
-                      f"2x2x1 cavity config, 4 timed steps after 1 warm-up ({dt:.1f} s)"}
+            "sample": f"oracle port (C, OpenMP) of the reference kernels on the same 256^3 2x2x1 cavity, "
+                      f"{steps} timed steps after 2 warm-up steps ({dt:.1f} s)"}
 
 
 def run_reference(args):
@@ -216,16 +219,70 @@ def config_dict(note=None):
     d = {"workload": "lid-driven cavity 256^3, 2x2x1 subdomains of 128x128x256 on one GPU, D3Q19 BGK + "
                      "Smagorinsky Cs=0.17, Re=10000, lid u=0.1, seeded start-up +-1e-3",
          "size": list(SIZE), "subdomains": list(NUMS), "storage": "f32", "cs": CS, "re": RE, "lid": U_LID,
-         "l2": "inputs larger than L2 (1.27 GB of populations per step vs 129 MB L2)"}
+         "l2": "inputs larger than L2 (1.27 GB of populations per step vs 129 MB L2)",
+         "halo": "after beta the 5 inward populations (reference); after alpha the 5 populations the ghost "
+                 "layer's inner neighbours gather (fluid and lid cells identical to the 19-population exchange)"}
     if note:
         d["note"] = note
     return d
 
 
 # ------------------------------------------------------------------ GPU arm
+def make_params(api, storage):
+    import numpy as np
+
+    pp = lattice_params(np.float64 if storage == "f64" else np.float32)
+    return api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
+
+
+def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None):
+    """K timed steps of one domain with a CUDA-event pair around every step
+    kernel; returns (wall ms of the K steps, step-kernel ms per launch,
+    graph-replay MLUPS, cells)."""
+    import torch
+
+    D = api.Domain(size, nums, api.STORAGE_NAMES[storage], store_velocity=False, store_density=False)
+    D.set_params(make_params(api, storage))
+    D.set_halo_mode(HALO_MODE)
+    D.reset()
+    D.perturb(SEED, AMP)
+    D.run(warmup, use_graph=False)
+    D.profile(True)
+    D.kernel_time(reset=True)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        start.record()
+        D.run(steps, use_graph=False)
+        stop.record()
+        torch.cuda.synchronize()
+    ms = start.elapsed_time(stop)
+    k_ms, k_n = D.kernel_time(reset=True)
+    D.profile(False)
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    D.run(steps, use_graph=True)
+    g1.record()
+    torch.cuda.synchronize()
+    cells = D.cells
+    graph_mlups = cells * steps / (g0.elapsed_time(g1) * 1e-3) / 1e6
+    del D
+    return ms, k_ms / max(1, k_n), graph_mlups, cells
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
-    import numpy as np
     import torch
 
     torch.cuda.set_device(local)
@@ -236,63 +293,42 @@ def run_gpu(args):
         build.build()
     if dist:
         dist.barrier()
-    pp = lattice_params(np.float32)
-    prm = api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
 
-    D = api.Domain(args.size, args.nums, api.F32, store_velocity=False, store_density=False)
-    D.set_params(prm)
-    D.reset()
-    D.perturb(SEED, AMP)
-    D.run(args.warmup, use_graph=False)
-    torch.cuda.synchronize()
-
-    # timed region: eager steps with one CUDA-event pair around every step kernel
-    D.profile(True)
-    D.kernel_time(reset=True)
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        start.record()
-        D.run(args.steps, use_graph=False)
-        stop.record()
-        torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    ms = start.elapsed_time(stop)
-    k_ms, k_n = D.kernel_time(reset=True)
-    D.profile(False)
+        ms, k_ms, graph_mlups, cells = measure(api, args.size, args.nums, "f32", args.steps, args.warmup, dist)
     ms = max_over_ranks(ms, dist)
-    cells = D.cells
     mlups = whole_job_mlups(cells, args.steps, ms, ws)
     if args.steps < 2:
         raise SystemExit("need at least 2 timed steps")
 
-    # the same with CUDA-graph replay of step pairs
-    torch.cuda.synchronize()
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record()
-    D.run(args.steps, use_graph=True)
-    g1.record()
-    torch.cuda.synchronize()
-    graph_mlups = cells * args.steps / (g0.elapsed_time(g1) * 1e-3) / 1e6
-
     # roofline of the step kernel
     peak, peak_kind = measured_peak()
-    per_launch_ms = k_ms / max(1, k_n)
     alg_bytes = BYTES_PER_CELL["f32"] * cells
-    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     traffic = profiled_traffic()
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": round(traffic * cells) if traffic else None,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6.8 TB/s", "kernel": "k_beta/k_alpha<float,LES> (step kernel)",
-                "kernel_ms_per_launch": round(per_launch_ms, 4), "alg_bytes_per_launch": alg_bytes}
-    del D
+                "kernel_ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": alg_bytes}
 
-    # e2e through the C ABI with host buffers
+    prm = make_params(api, "f32")
     e2e = None if args.no_e2e else run_e2e(api, prm, args.steps)
+
+    extra = {}
+    if not args.no_extra and tuple(args.size) == SIZE:
+        n = max(50, min(args.steps, 400))
+        for label, size, nums, st in (("f64 256^3 2x2x1", SIZE, NUMS, "f64"),
+                                      ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16"),
+                                      ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16"),
+                                      ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32"),
+                                      ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16")):
+            xms, xk, xg, xc = measure(api, size, nums, st, n, 4)
+            xa = BYTES_PER_CELL[st] * xc / (xk * 1e-3) / 1e9
+            extra[label] = {"mlups": round(xc * n / (xms * 1e-3) / 1e6, 1), "graph_mlups": round(xg, 1),
+                            "kernel_ms": round(xk, 4), "achieved_gbs": round(xa, 1),
+                            "frac_of_measured_hbm": round(xa / peak, 4), "steps": n,
+                            "alg_bytes_per_cell": BYTES_PER_CELL[st]}
 
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
@@ -304,6 +340,8 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "graph_mlups": round(graph_mlups, 1),
     }
+    if extra:
+        line["extra"] = extra
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0:
@@ -320,6 +358,7 @@ def run_e2e(api, prm, steps):
 
     D = api.Domain(SIZE, NUMS, api.F32, store_velocity=True, store_density=False)
     D.set_params(prm)
+    D.set_halo_mode(HALO_MODE)
     D.reset()
     D.perturb(SEED, AMP)
     D.set_store_interval(0)  # velocity written on the last step only
@@ -364,6 +403,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the extra storage / size measurements")
     ap.add_argument("--size", type=int, nargs=3, default=list(SIZE), help="domain size (profiling only)")
     ap.add_argument("--nums", type=int, nargs=3, default=list(NUMS), help="subdomains (profiling only)")
     args = ap.parse_args()

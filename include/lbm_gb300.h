@@ -157,6 +157,13 @@ int lbm_cu_domain_run(lbm_domain *dom, int steps, int use_graph, void *stream);
  * (the default); interval 0 writes them only on the last step of each
  * lbm_cu_domain_run call. */
 int lbm_cu_domain_set_store_interval(lbm_domain *dom, int interval);
+/* Populations exchanged after an alpha step: mode 0 copies all 19 of the
+ * neighbour's inner layer into the ghost layer, as syncAlpha does
+ * (src/CController.hpp:265-320); mode 1 copies only the 5 that the ghost
+ * layer's inner neighbours gather in the next beta step (direction . e < 0).
+ * Both give identical fluid, lid and wall cells; ghost-layer populations
+ * differ in the 14 slots no other cell reads. */
+int lbm_cu_domain_set_halo_mode(lbm_domain *dom, int mode);
 /* Time every step-kernel launch with a pair of CUDA events on the launching
  * stream (steps then run without graph replay), and read the accumulated
  * milliseconds and launch count (reset != 0 clears them).  Stands in for the

@@ -23,7 +23,8 @@
  * Hou, Sterling, Chen & Doolen (1996), "A lattice Boltzmann subgrid model for
  * high Reynolds number flows": the total relaxation time per cell is
  *     tau_eff = (tau0 + sqrt(tau0^2 + C * sqrt(Q))) / 2,
- *     Q = Pi_ab Pi_ab,  Pi_ab = sum_i e_ia e_ib (f_i - f_i^eq),
+ *     Q = Pi_ab Pi_ab,  Pi_ab = sum_i e_ia e_ib (f_i - f_i^eq)
+ *                             = sum_i e_ia e_ib f_i - rho/3 delta_ab - u_a u_b,
  *     C = 18 * sqrt(2) * Cs^2  (lattice units, Delta = 1, rho0 = 1 of the
  *                               incompressible equilibrium),
  * inserted into the reference BGK update in place of the constant inv_tau.
@@ -194,32 +195,40 @@ static void equilibria(REAL vx, REAL vy, REAL vz, REAL dp, REAL eq[19]) {
 }
 
 /* Relaxation rate for one cell: the constant inv_tau when the subgrid model
- * is off (les_c == 0, identical to the reference), else the Smagorinsky rate
- * from the non-equilibrium stress of d[i] = eq[i] - f[i]. */
-static inline REAL relax_rate(const REAL d[19], REAL inv_tau, REAL tau0, REAL les_c) {
+ * is off (les_c == 0, identical to the reference), else the Smagorinsky rate.
+ * The non-equilibrium stress is taken from moments of the pre-collision
+ * populations, Pi_ab = sum_i e_ia e_ib f_i - rho/3 delta_ab - u_a u_b (the
+ * second moment of the incompressible equilibrium is rho/3 delta + u u),
+ * built from the nine opposite-pair sums p_k = f_2k + f_2k+1. */
+static inline REAL relax_rate(const REAL f[19], REAL rho, REAL vx, REAL vy, REAL vz, REAL inv_tau, REAL tau0,
+                              REAL les_c) {
     if (les_c == (REAL)0) return inv_tau;
-    REAL s[9];
-    for (int k = 0; k < 9; k++) s[k] = d[2 * k] + d[2 * k + 1];
-    REAL pxx = (((s[0] + s[2]) + s[3]) + s[4]) + s[5];
-    REAL pyy = (((s[1] + s[2]) + s[3]) + s[6]) + s[7];
-    REAL pzz = (((s[4] + s[5]) + s[6]) + s[7]) + s[8];
-    REAL pxy = s[2] - s[3];
-    REAL pxz = s[4] - s[5];
-    REAL pyz = s[6] - s[7];
+    REAL p[9];
+    for (int k = 0; k < 9; k++) p[k] = f[2 * k] + f[2 * k + 1];
+    REAL sxx = (((p[0] + p[2]) + p[3]) + p[4]) + p[5];
+    REAL syy = (((p[1] + p[2]) + p[3]) + p[6]) + p[7];
+    REAL szz = (((p[4] + p[5]) + p[6]) + p[7]) + p[8];
+    REAL r3 = rho * C3;
+    REAL pxx = (sxx - r3) - vx * vx;
+    REAL pyy = (syy - r3) - vy * vy;
+    REAL pzz = (szz - r3) - vz * vz;
+    REAL pxy = (p[2] - p[3]) - vx * vy;
+    REAL pxz = (p[4] - p[5]) - vx * vz;
+    REAL pyz = (p[6] - p[7]) - vy * vz;
     REAL q = ((pxx * pxx + pyy * pyy) + pzz * pzz) + (REAL)2 * ((pxy * pxy + pxz * pxz) + pyz * pyz);
     REAL te = (REAL)0.5 * (tau0 + RSQRT(tau0 * tau0 + les_c * RSQRT(q)));
     return (REAL)1 / te;
 }
 
 /* BGK collision of a FLUID cell, f updated in place: lbm_beta.cl:497-559 /
- * lbm_alpha.cl:179-303 without the gravity terms. */
-static void collide(REAL f[19], REAL vx, REAL vy, REAL vz, REAL dp, REAL inv_tau, REAL tau0,
+ * lbm_alpha.cl:179-303 without the gravity terms.  rho is the population
+ * sum (before the reference aliases it), dp the equilibrium's dd_param. */
+static void collide(REAL f[19], REAL rho, REAL vx, REAL vy, REAL vz, REAL dp, REAL inv_tau, REAL tau0,
                     REAL les_c) {
-    REAL eq[19], d[19];
+    REAL eq[19];
+    REAL w = relax_rate(f, rho, vx, vy, vz, inv_tau, tau0, les_c);
     equilibria(vx, vy, vz, dp, eq);
-    for (int i = 0; i < 19; i++) d[i] = eq[i] - f[i];
-    REAL w = relax_rate(d, inv_tau, tau0, les_c);
-    for (int i = 0; i < 19; i++) f[i] += w * d[i];
+    for (int i = 0; i < 19; i++) f[i] += w * (eq[i] - f[i]);
 }
 
 /* The alpha kernel's gravity terms.  The reference aliases its temporary to
@@ -304,7 +313,7 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
         if (fl == FL_FLUID) {
             REAL v2 = (vx * vx + vy * vy) + vz * vz;
             REAL dp = r - K15 * v2;
-            collide(f, vx, vy, vz, dp, inv_tau, tau0, les_c);
+            collide(f, r, vx, vy, vz, dp, inv_tau, tau0, les_c);
             r = gravity_chain(r, gx, gy, gz, t);
             write = 1;
         } else if (fl == FL_OBSTACLE) {
@@ -373,8 +382,9 @@ void SFX(orc_beta)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_t
         r += f[18];
         if (fl == FL_FLUID) {
             REAL v2 = (vx * vx + vy * vy) + vz * vz;
-            r = r - K15 * v2; /* dd_param aliases rho: lbm_beta.cl:493 */
-            collide(f, vx, vy, vz, r, inv_tau, tau0, les_c);
+            REAL dp = r - K15 * v2;
+            collide(f, r, vx, vy, vz, dp, inv_tau, tau0, les_c);
+            r = dp; /* dd_param aliases rho: lbm_beta.cl:493 */
         } else if (fl == FL_OBSTACLE) {
             vx = 0; vy = 0; vz = 0;
             for (int k = 0; k < 9; k++) { /* bounce back: lbm_beta.cl:570-578 */

@@ -345,8 +345,9 @@ class Domain:
 
     `kernels_for(dims)` returns a kernel back-end for a subdomain size."""
 
-    def __init__(self, kernels_for, size, nums, params: Params, storage="f32", lid_geometry=True):
+    def __init__(self, kernels_for, size, nums, params: Params, storage="f32", lid_geometry=True, halo_mode=0):
         self.p = params
+        self.halo_mode = halo_mode  # 1: after alpha only the populations gathered inward
         self.sub, layout = manager_layout(size, nums)
         self.nums = tuple(nums)
         self.parts = []
@@ -405,6 +406,9 @@ class Domain:
                     if beta:   # unpack into the inner layer, inward populations only
                         sel = [f for f in range(19) if int(np.dot(cm.direction, E[f])) > 0]
                         s.lat.dd[(sel,) + region(cm.send_origin, cm.send_size)] = buf[sel]
+                    elif self.halo_mode:  # the ghost populations the inner neighbours gather
+                        sel = [f for f in range(19) if int(np.dot(cm.direction, E[f])) < 0]
+                        s.lat.dd[(sel,) + region(cm.recv_origin, cm.recv_size)] = buf[sel]
                     else:
                         s.lat.dd[(slice(None),) + region(cm.recv_origin, cm.recv_size)] = buf
 

@@ -167,16 +167,19 @@ def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph):
         assert got == ref[done - 1], f"step {done}"
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16"])
-def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage):
+@pytest.mark.parametrize("storage,nums,halo_mode", [("f32", (2, 2, 1), 0), ("f64", (2, 2, 1), 0),
+                                                    ("f16", (2, 2, 1), 0), ("f32", (3, 2, 2), 1),
+                                                    ("bf16", (2, 1, 3), 1)])
+def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, nums, halo_mode):
     api, O = capi, oracle_mod
-    size, nums = (30, 20, 12), (2, 2, 1)
+    size = (30, 20, 12) if nums == (2, 2, 1) else (36, 24, 24)
     p = oracle_params(O, storage, (28, 0, 0), cs=0.17, re=5000.0, u=0.1)
     D = api.Domain(size, nums, api.STORAGE_NAMES[storage], True, True)
     D.set_params(gpu_params(api, p))
+    D.set_halo_mode(halo_mode)
     D.reset()
     D.perturb(SEED, 1e-2)
-    R = O.Domain(lambda d: O.OracleKernels(storage), size, nums, p, storage)
+    R = O.Domain(lambda d: O.OracleKernels(storage), size, nums, p, storage, halo_mode=halo_mode)
     R.perturb(SEED, 1e-2)
     for _ in range(3):
         D.run(5, True)

@@ -142,6 +142,26 @@ def test_decomposition_equals_single_domain(oracle_mod):
             assert n_diff(loc, glob) == 0
 
 
+def test_minimal_halo_changes_only_ghost_populations(oracle_mod):
+    """Exchanging after alpha only the 5 populations the ghost layer's inner
+    neighbours gather leaves every fluid and lid cell bit-identical (wall
+    cells differ only in the outward, wrap-dependent slots)."""
+    O = oracle_mod
+    p = O.Params.lattice(O.cavity_tau(0.1, 40, 5000.0), 0.1, 0.17, dtype=np.float32)
+    size, nums = (42, 30, 24), (3, 2, 2)
+    A = O.Domain(lambda d: O.OracleKernels("f32"), size, nums, p, "f32")
+    B = O.Domain(lambda d: O.OracleKernels("f32"), size, nums, p, "f32", halo_mode=1)
+    for D in (A, B):
+        D.perturb(SEED, 1e-2)
+    for _ in range(30):
+        A.step()
+        B.step()
+        for (_, a, _), (_, b, _) in zip(A.parts, B.parts):
+            keep = O.fluid_mask(a.lat.flags)
+            assert n_diff(a.lat.dd[:, keep], b.lat.dd[:, keep]) == 0
+            assert n_diff(a.lat.vel, b.lat.vel) == 0 and n_diff(a.lat.rho[keep], b.lat.rho[keep]) == 0
+
+
 # ------------------------------------------------------- subgrid model pins
 def _np_les_alpha(f, tau0, les_c):
     """Independent float64 statement of one alpha collision with the
@@ -158,8 +178,10 @@ def _np_les_alpha(f, tau0, les_c):
     u2 = (j ** 2).sum(0)
     dp = rho - 1.5 * u2
     feq = w[:, None] * (dp + 3 * eu + 4.5 * eu ** 2)
-    neq = f - feq
-    pi = np.einsum("ia,ib,i...->ab...", e, e, neq)
+    # Pi^neq = sum e e f - (rho/3 delta + u u), the incompressible equilibrium's second moment
+    third = float(np.float32(1 / 3))  # the constant as the kernels write it, (T)(1.0f/3.0f)
+    pi = np.einsum("ia,ib,i...->ab...", e, e, f) - np.einsum("ab,...->ab...", np.eye(3), rho * third) \
+        - np.einsum("a...,b...->ab...", j, j)
     q = (pi ** 2).sum((0, 1))
     te = 0.5 * (tau0 + np.sqrt(tau0 ** 2 + les_c * np.sqrt(q)))
     return f + (feq - f) / te

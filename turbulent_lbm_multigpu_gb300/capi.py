@@ -80,6 +80,7 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_run": ([vp, ci, ci, vp], ci),
         "lbm_cu_domain_counter": ([vp, C.POINTER(i64)], ci),
         "lbm_cu_domain_set_store_interval": ([vp, ci], ci),
+        "lbm_cu_domain_set_halo_mode": ([vp, ci], ci),
         "lbm_cu_domain_profile": ([vp, ci], ci),
         "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
@@ -237,6 +238,10 @@ class Domain:
 
     def set_store_interval(self, interval: int):
         check(lib().lbm_cu_domain_set_store_interval(self.h, interval))
+
+    def set_halo_mode(self, mode: int):
+        """0: all 19 populations after alpha (reference); 1: the 5 read inward."""
+        check(lib().lbm_cu_domain_set_halo_mode(self.h, mode))
 
     def profile(self, enable: bool):
         check(lib().lbm_cu_domain_profile(self.h, int(enable)))

@@ -78,13 +78,6 @@ int ensure_stage(lbm_lattice *l, size_t bytes) {
     return 0;
 }
 
-int upload_desc(lbm_lattice *l, cudaStream_t st) {
-    if (!l->dirty) return 0;
-    CU(cudaMemcpyAsync(l->d_desc, &l->h, sizeof(LatDesc), cudaMemcpyHostToDevice, st));
-    l->dirty = false;
-    return 0;
-}
-
 // Parameters rounded to the arithmetic type R, plus the gravity chain
 // coefficients of lbm_alpha.cl:183-291 computed in R.
 template <typename R> void fill_params(const lbm_params &p, R out[16], int *grav) {
@@ -199,54 +192,83 @@ __global__ void k_perturb(LatDesc d, int ox, int oy, int oz, int gx, int gy, int
     if (store_rho) ((R *)d.rho)[c] = (R)1.0f;
 }
 
-// Box copy between a lattice field and a packed [plane][z][y][x] buffer.
-struct Box {
-    int64_t lat_nx, lat_slice;   // lattice geometry
-    int ox, oy, oz, sx, sy, sz;  // rectangle
-    int64_t cells;               // sx*sy*sz
-    uint32_t mask;               // planes to copy
-    int nplanes;
+// Exact quotient of a 32-bit unsigned n by an invariant d >= 1 with one
+// multiply-high and two shifts (Granlund & Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994, figure 4.1).
+struct FastDiv {
+    uint32_t d, m, s1, s2;
+    static FastDiv make(uint32_t d) {
+        FastDiv f;
+        uint32_t l = 0;
+        while ((1ull << l) < d) l++;
+        f.d = d;
+        f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+        f.s1 = l < 1 ? l : 1;
+        f.s2 = l > 1 ? l - 1 : 0;
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        const uint32_t t = __umulhi(m, n);
+        return (t + ((n - t) >> s1)) >> s2;
+    }
 };
 
-__device__ __forceinline__ int64_t box_cell(const Box &b, int64_t k) {
-    const int64_t x = k % b.sx, y = (k / b.sx) % b.sy, z = k / ((int64_t)b.sx * b.sy);
-    return (b.oz + z) * b.lat_slice + (b.oy + y) * b.lat_nx + (b.ox + x);
+// A rectangle of a lattice: origin, size, and the lattice's row/slice pitch.
+struct Box {
+    int64_t lat_nx, lat_slice;
+    int ox, oy, oz, sx, sy, sz;
+    int64_t cells;
+    FastDiv dx, dy;
+};
+
+__device__ __forceinline__ int64_t box_cell(const Box &b, uint32_t k) {
+    const uint32_t r = b.dx.div(k);
+    const uint32_t x = k - r * b.sx;
+    const uint32_t z = b.dy.div(r);
+    const uint32_t y = r - z * b.sy;
+    return (int64_t)(b.oz + z) * b.lat_slice + (int64_t)(b.oy + y) * b.lat_nx + (b.ox + x);
 }
 
-// Populations: decode to the arithmetic type (pack) or encode (unpack).
+// Up to 19 population planes to copy.
+struct Planes {
+    uint8_t f[20];
+    int n;
+};
+
+// Populations between the lattice and a packed [plane][z][y][x] buffer of
+// the arithmetic type: decoded when packing, encoded when unpacking.
+// grid.y = index into the plane list.
 template <typename S, bool PACK>
-__global__ void k_box_dd(S *dd, int64_t pstride, typename Store<S>::R *buf, Box b) {
+__global__ void k_box_dd(S *dd, int64_t pstride, typename Store<S>::R *buf, Box b, Planes pl) {
     using R = typename Store<S>::R;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= b.cells * 19) return;
-    const int f = (int)(t / b.cells);
-    if (!((b.mask >> f) & 1u)) return;
-    const int64_t k = t - (int64_t)f * b.cells;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= b.cells) return;
+    const int f = pl.f[blockIdx.y];
     S *p = dd + f * pstride + box_cell(b, k);
-    R w = weight<R>(f);
-    if (PACK) buf[t] = Store<S>::ld(p, w);
-    else Store<S>::st(p, buf[t], w);
+    const int64_t t = (int64_t)f * b.cells + k;
+    if (PACK) buf[t] = Store<S>::ld(p, weight<R>(f));
+    else Store<S>::st(p, buf[t], weight<R>(f));
 }
 
 // Velocity / density planes: plain copies.
 template <typename R, bool PACK>
 __global__ void k_box_real(R *field, int64_t pstride, R *buf, Box b) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= b.cells * b.nplanes) return;
-    const int f = (int)(t / b.cells);
-    const int64_t k = t - (int64_t)f * b.cells;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= b.cells) return;
+    const int f = blockIdx.y;
     R *p = field + f * pstride + box_cell(b, k);
+    const int64_t t = (int64_t)f * b.cells + k;
     if (PACK) buf[t] = *p;
     else *p = buf[t];
 }
 
 template <bool PACK>
 __global__ void k_box_flags(uint8_t *flags, int32_t *buf, Box b) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= b.cells) return;
-    uint8_t *p = flags + box_cell(b, t);
-    if (PACK) buf[t] = *p;
-    else *p = (uint8_t)buf[t];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= b.cells) return;
+    uint8_t *p = flags + box_cell(b, k);
+    if (PACK) buf[k] = *p;
+    else *p = (uint8_t)buf[k];
 }
 
 __global__ void k_check_flags(const int32_t *buf, int64_t cells, int *bad) {
@@ -254,41 +276,32 @@ __global__ void k_check_flags(const int32_t *buf, int64_t cells, int *bad) {
     if (t < cells && (buf[t] < 0 || buf[t] > 255)) *bad = 1;
 }
 
-// Batched halo copies: every copy of one axis phase in one launch.
+// Halo copy between two lattices of the same storage: raw elements of the
+// selected planes.  grid = (cells, plane list index, copy index).
 struct HaloDesc {
     void *src, *dst;
     int64_t sps, dps;
     Box sb, db;
-    int64_t first;  // first flat index of this copy
+    Planes pl;
 };
 
-// One halo copy element: the j-th selected plane of cell k of the box.
 template <typename E>
-__device__ __forceinline__ void halo_elem(const HaloDesc &h, int64_t u) {
-    const int j = (int)(u / h.sb.cells);
-    const int64_t k = u - (int64_t)j * h.sb.cells;
-    uint32_t m = h.sb.mask;
-    for (int q = 0; q < j; q++) m &= m - 1;
-    const int f = __ffs(m) - 1;
+__device__ __forceinline__ void halo_elem(const HaloDesc &h) {
+    if ((int)blockIdx.y >= h.pl.n) return;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= h.sb.cells) return;
+    const int f = h.pl.f[blockIdx.y];
     ((E *)h.dst)[f * h.dps + box_cell(h.db, k)] = ((const E *)h.src)[f * h.sps + box_cell(h.sb, k)];
 }
 
 template <typename E>
-__global__ void k_halo_one(HaloDesc h, int64_t total) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < total) halo_elem<E>(h, t);
+__global__ void k_halo_one(HaloDesc h) {
+    halo_elem<E>(h);
 }
 
 template <typename E>
-__global__ void k_halo_batch(const HaloDesc *__restrict__ hd, int nd, int64_t total) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= total) return;
-    int lo = 0, hi = nd - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (hd[mid].first <= t) lo = mid; else hi = mid - 1;
-    }
-    halo_elem<E>(hd[lo], t - hd[lo].first);
+__global__ void k_halo_batch(const HaloDesc *__restrict__ hd) {
+    halo_elem<E>(hd[blockIdx.z]);
 }
 
 // Neumaier-compensated FP64 accumulation.
@@ -360,74 +373,88 @@ __global__ void k_reduce_final(const double *partial, int nblocks, double *out) 
 
 // ------------------------------------------------------------- dispatchers
 template <typename S>
-int launch_step_t(int parity, bool les, const LatDesc *tab, int ntab, int blocks, int sv, int sr, cudaStream_t st) {
+int launch_step_t(int parity, bool les, const StepArgs &a, int blocks, cudaStream_t st) {
     if (blocks <= 0) return 0;
+    const bool pt = a.ntab <= kParamLattices;
+#define STEP(K_, L_, P_) K_<S, L_, P_><<<blocks, kBlock, 0, st>>>(a)
     if (parity) {
-        if (les) k_alpha<S, true><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
-        else k_alpha<S, false><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+        if (les) { if (pt) STEP(k_alpha, true, true); else STEP(k_alpha, true, false); }
+        else { if (pt) STEP(k_alpha, false, true); else STEP(k_alpha, false, false); }
     } else {
-        if (les) k_beta<S, true><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
-        else k_beta<S, false><<<blocks, kBlock, 0, st>>>(tab, ntab, sv, sr);
+        if (les) { if (pt) STEP(k_beta, true, true); else STEP(k_beta, true, false); }
+        else { if (pt) STEP(k_beta, false, true); else STEP(k_beta, false, false); }
     }
+#undef STEP
     CU(cudaGetLastError());
     return 0;
 }
 
-int launch_step(int storage, int parity, bool les, const LatDesc *tab, int ntab, int blocks, int sv, int sr,
-                cudaStream_t st) {
+// One step over `ntab` lattices: descriptors from the host copy `htab`
+// (kernel parameters when they fit), else from the device table `dtab`.
+int launch_step(int storage, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab, int blocks,
+                int sv, int sr, cudaStream_t st) {
+    StepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.ntab = ntab;
+    a.dtab = dtab;
+    a.store_v = sv;
+    a.store_rho = sr;
+    if (ntab <= kParamLattices)
+        for (int i = 0; i < ntab; i++) a.tab[i] = htab[i];
     switch (storage) {
-        case kF32: return launch_step_t<float>(parity, les, tab, ntab, blocks, sv, sr, st);
-        case kF64: return launch_step_t<double>(parity, les, tab, ntab, blocks, sv, sr, st);
-        case kF16: return launch_step_t<__half>(parity, les, tab, ntab, blocks, sv, sr, st);
-        case kBF16: return launch_step_t<__nv_bfloat16>(parity, les, tab, ntab, blocks, sv, sr, st);
+        case kF32: return launch_step_t<float>(parity, les, a, blocks, st);
+        case kF64: return launch_step_t<double>(parity, les, a, blocks, st);
+        case kF16: return launch_step_t<__half>(parity, les, a, blocks, st);
+        case kBF16: return launch_step_t<__nv_bfloat16>(parity, les, a, blocks, st);
     }
     return fail("unknown storage type");
 }
 
 int grid_for(int64_t work) { return (int)((work + kBlock - 1) / kBlock); }
 
-Box make_box(const lbm_lattice *l, const int o[3], const int s[3], uint32_t mask) {
+Box make_box(const lbm_lattice *l, const int o[3], const int s[3]) {
     Box b;
     b.lat_nx = l->nx;
     b.lat_slice = (int64_t)l->nx * l->ny;
     b.ox = o[0]; b.oy = o[1]; b.oz = o[2];
     b.sx = s[0]; b.sy = s[1]; b.sz = s[2];
     b.cells = (int64_t)s[0] * s[1] * s[2];
-    b.mask = mask;
-    b.nplanes = __builtin_popcount(mask);
+    b.dx = FastDiv::make(s[0] > 0 ? s[0] : 1);
+    b.dy = FastDiv::make(s[1] > 0 ? s[1] : 1);
     return b;
 }
 
-uint32_t norm_mask(const int norm[3]) {
-    if (!norm) return (1u << 19) - 1;
-    uint32_t m = 0;
+// Planes f with sign * (norm . e_f) > 0, or all 19 when norm is null.
+Planes plane_list(const int norm[3], int sign = 1) {
+    Planes p;
+    p.n = 0;
     for (int f = 0; f < 19; f++)
-        if (norm[0] * dir_x(f) + norm[1] * dir_y(f) + norm[2] * dir_z(f) > 0) m |= 1u << f;
-    return m;
+        if (!norm || sign * (norm[0] * dir_x(f) + norm[1] * dir_y(f) + norm[2] * dir_z(f)) > 0) p.f[p.n++] = (uint8_t)f;
+    return p;
+}
+
+dim3 halo_grid(int64_t cells, int planes, int copies) {
+    return dim3((unsigned)((cells + kBlock - 1) / kBlock), (unsigned)planes, (unsigned)copies);
 }
 
 template <typename E>
-int launch_halo(const HaloDesc *d_hd, int nd, int64_t total, cudaStream_t st) {
-    if (total <= 0) return 0;
-    k_halo_batch<E><<<grid_for(total), kBlock, 0, st>>>(d_hd, nd, total);
+int launch_halo_one(const HaloDesc &h, cudaStream_t st) {
+    k_halo_one<E><<<halo_grid(h.sb.cells, h.pl.n, 1), kBlock, 0, st>>>(h);
     CU(cudaGetLastError());
     return 0;
 }
 
-template <typename E>
-int launch_halo_one(const HaloDesc &h, int64_t total, cudaStream_t st) {
-    k_halo_one<E><<<grid_for(total), kBlock, 0, st>>>(h, total);
-    CU(cudaGetLastError());
-    return 0;
-}
-
-int launch_halo_any(int storage, const HaloDesc *d_hd, int nd, int64_t total, cudaStream_t st) {
+// All copies of one exchange phase in one launch.
+int launch_halo_batch(int storage, const HaloDesc *d_hd, int nd, int64_t max_cells, int max_planes, cudaStream_t st) {
+    if (nd <= 0 || max_cells <= 0) return 0;
+    const dim3 g = halo_grid(max_cells, max_planes, nd);
     switch (storage_bytes(storage)) {
-        case 2: return launch_halo<uint16_t>(d_hd, nd, total, st);
-        case 4: return launch_halo<uint32_t>(d_hd, nd, total, st);
-        case 8: return launch_halo<uint64_t>(d_hd, nd, total, st);
+        case 2: k_halo_batch<uint16_t><<<g, kBlock, 0, st>>>(d_hd); break;
+        case 4: k_halo_batch<uint32_t><<<g, kBlock, 0, st>>>(d_hd); break;
+        default: k_halo_batch<uint64_t><<<g, kBlock, 0, st>>>(d_hd); break;
     }
-    return fail("bad storage size");
+    CU(cudaGetLastError());
+    return 0;
 }
 }  // namespace
 
@@ -546,9 +573,8 @@ int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t see
 
 int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
     if (!l) return fail("NULL lattice");
-    if (upload_desc(l, S(stream))) return -1;
-    return launch_step(l->storage, parity & 1, uses_les(l->h), l->d_desc, 1, l->h.nblocks, l->store_v, l->store_rho,
-                       S(stream));
+    return launch_step(l->storage, parity & 1, uses_les(l->h), &l->h, nullptr, 1, l->h.nblocks, l->store_v,
+                       l->store_rho, S(stream));
 }
 
 static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], void *host, const int norm[3],
@@ -576,15 +602,17 @@ static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], voi
         default: return fail("unknown field");
     }
     const size_t bytes = (size_t)cells * nplanes * ebytes;
+    if (cells > INT32_MAX) return fail("rectangle has more than 2^31-1 cells");
     if (ensure_stage(l, bytes + 256)) return -1;
-    const uint32_t mask = field == LBM_FIELD_DD ? norm_mask(read ? nullptr : norm) : (1u << nplanes) - 1;
-    Box b = make_box(l, o, s, mask);
+    Box b = make_box(l, o, s);
     if (!read) CU(cudaMemcpyAsync(l->stage, host, bytes, cudaMemcpyHostToDevice, st));
-    const int g = grid_for(cells * nplanes);
+    const unsigned gx = (unsigned)((cells + kBlock - 1) / kBlock);
     if (field == LBM_FIELD_DD) {
+        const Planes pl = plane_list(read ? nullptr : norm);
+        const dim3 g(gx, (unsigned)pl.n);
 #define BOX(S_, R_)                                                                                          \
-    (read ? k_box_dd<S_, true><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b)             \
-          : k_box_dd<S_, false><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b))
+    (read ? k_box_dd<S_, true><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b, pl)         \
+          : k_box_dd<S_, false><<<g, kBlock, 0, st>>>((S_ *)l->dd, l->pstride, (R_ *)l->stage, b, pl))
         switch (l->storage) {
             case kF32: BOX(float, float); break;
             case kF64: BOX(double, double); break;
@@ -601,12 +629,13 @@ static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], voi
             CU(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
             CU(cudaStreamSynchronize(st));
             if (hbad) return fail("flag values must lie in [0, 255]");
-            k_box_flags<false><<<g, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
+            k_box_flags<false><<<gx, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
         } else {
-            k_box_flags<true><<<g, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
+            k_box_flags<true><<<gx, kBlock, 0, st>>>(l->flags, (int32_t *)l->stage, b);
         }
     } else {
         void *fieldp = field == LBM_FIELD_VELOCITY ? l->vel : l->rho;
+        const dim3 g(gx, (unsigned)nplanes);
         if (rb == 8) {
             if (read) k_box_real<double, true><<<g, kBlock, 0, st>>>((double *)fieldp, l->n, (double *)l->stage, b);
             else k_box_real<double, false><<<g, kBlock, 0, st>>>((double *)fieldp, l->n, (double *)l->stage, b);
@@ -638,19 +667,18 @@ int lbm_cu_halo(lbm_lattice *src, const int so[3], lbm_lattice *dst, const int d
     if (!src || !dst || !so || !dof || !size) return fail("NULL argument");
     if (src->storage != dst->storage) return fail("halo copy between lattices of different storage");
     if (!valid_box(src, so, size) || !valid_box(dst, dof, size)) return fail("halo rectangle outside a lattice");
-    const uint32_t mask = norm_mask(norm);
     HaloDesc h;
     h.src = src->dd; h.dst = dst->dd;
     h.sps = src->pstride; h.dps = dst->pstride;
-    h.sb = make_box(src, so, size, mask);
-    h.db = make_box(dst, dof, size, mask);
-    h.first = 0;
-    const int64_t total = h.sb.cells * h.sb.nplanes;
-    if (total == 0) return 0;
+    h.sb = make_box(src, so, size);
+    h.db = make_box(dst, dof, size);
+    h.pl = plane_list(norm);
+    if (h.sb.cells == 0) return 0;
+    if (h.sb.cells > INT32_MAX) return fail("halo rectangle has more than 2^31-1 cells");
     switch (storage_bytes(src->storage)) {
-        case 2: return launch_halo_one<uint16_t>(h, total, S(stream));
-        case 4: return launch_halo_one<uint32_t>(h, total, S(stream));
-        default: return launch_halo_one<uint64_t>(h, total, S(stream));
+        case 2: return launch_halo_one<uint16_t>(h, S(stream));
+        case 4: return launch_halo_one<uint32_t>(h, S(stream));
+        default: return launch_halo_one<uint64_t>(h, S(stream));
     }
 }
 
@@ -693,12 +721,15 @@ struct lbm_domain {
     std::vector<std::vector<int>> bc;
     std::vector<int> coords;  // 3 per subdomain
     LatDesc *d_tab = nullptr;
+    std::vector<LatDesc> h_tab;
     int blocks = 0;
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
     std::vector<HaloDesc> plan[2][3];
     HaloDesc *d_plan[2][3] = {};
-    int64_t plan_total[2][3] = {};
+    int64_t plan_cells[2][3] = {};
+    int plan_planes[2][3] = {};
+    int halo_mode = 0;  // 0: all 19 populations after alpha (reference), 1: the 5 read inward
     int64_t counter = 0;
     int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
     cudaGraphExec_t graph = nullptr;
@@ -717,7 +748,8 @@ int domain_build_plans(lbm_domain *D) {
         for (int a = 0; a < 3; a++) {
             auto &v = D->plan[ph][a];
             v.clear();
-            int64_t first = 0;
+            int64_t cells = 0;
+            int planes = 0;
             for (size_t b = 0; b < D->subs.size(); b++) {
                 for (const CommGeom &cm : D->comms[b]) {
                     if (cm.axis != a) continue;
@@ -730,20 +762,26 @@ int domain_build_plans(lbm_domain *D) {
                     HaloDesc h;
                     h.src = A->dd; h.dst = B->dd;
                     h.sps = A->pstride; h.dps = B->pstride;
-                    if (ph == 1) {  // syncAlpha: neighbour's inner layer -> own ghost layer, 19 planes
-                        h.sb = make_box(A, back->send_origin, back->size, (1u << 19) - 1);
-                        h.db = make_box(B, cm.recv_origin, cm.size, (1u << 19) - 1);
-                    } else {        // syncBeta: neighbour's ghost layer -> own inner layer, inward planes
-                        const uint32_t m = norm_mask(cm.dir);
-                        h.sb = make_box(A, back->recv_origin, back->size, m);
-                        h.db = make_box(B, cm.send_origin, cm.size, m);
+                    if (ph == 1) {
+                        // syncAlpha: neighbour's inner layer -> own ghost layer.  All 19
+                        // populations as the reference, or only those the inner
+                        // neighbours of the ghost layer gather (direction . e < 0).
+                        h.sb = make_box(A, back->send_origin, back->size);
+                        h.db = make_box(B, cm.recv_origin, cm.size);
+                        h.pl = D->halo_mode ? plane_list(cm.dir, -1) : plane_list(nullptr);
+                    } else {
+                        // syncBeta: neighbour's ghost layer -> own inner layer, direction . e > 0
+                        h.sb = make_box(A, back->recv_origin, back->size);
+                        h.db = make_box(B, cm.send_origin, cm.size);
+                        h.pl = plane_list(cm.dir);
                     }
-                    h.first = first;
-                    first += h.sb.cells * h.sb.nplanes;
+                    cells = std::max<int64_t>(cells, h.sb.cells);
+                    planes = std::max(planes, h.pl.n);
                     v.push_back(h);
                 }
             }
-            D->plan_total[ph][a] = first;
+            D->plan_cells[ph][a] = cells;
+            D->plan_planes[ph][a] = planes;
             if (D->d_plan[ph][a]) {
                 cudaFree(D->d_plan[ph][a]);
                 D->d_plan[ph][a] = nullptr;
@@ -767,6 +805,7 @@ int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
         tab.push_back(h);
     }
     D->blocks = first;
+    D->h_tab = tab;
     CU(cudaMemcpyAsync(D->d_tab, tab.data(), tab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice, st));
     CU(cudaStreamSynchronize(st));
     D->tab_dirty = false;
@@ -789,11 +828,13 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
     const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (timed && domain_record(D, st, &e0)) return -1;
-    if (launch_step(D->storage, parity, les, D->d_tab, (int)D->subs.size(), D->blocks, sv, sr, st)) return -1;
+    if (launch_step(D->storage, parity, les, D->h_tab.data(), D->d_tab, (int)D->subs.size(), D->blocks, sv, sr, st))
+        return -1;
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
-        if (D->plan_total[parity][a] > 0 &&
-            launch_halo_any(D->storage, D->d_plan[parity][a], (int)D->plan[parity][a].size(), D->plan_total[parity][a], st))
+        if (!D->plan[parity][a].empty() &&
+            launch_halo_batch(D->storage, D->d_plan[parity][a], (int)D->plan[parity][a].size(), D->plan_cells[parity][a],
+                              D->plan_planes[parity][a], st))
             return -1;
     return 0;
 }
@@ -983,6 +1024,15 @@ int lbm_cu_domain_set_store_interval(lbm_domain *D, int interval) {
     if (interval < 0) return fail("negative store interval");
     D->store_interval = interval;
     return 0;
+}
+
+int lbm_cu_domain_set_halo_mode(lbm_domain *D, int mode) {
+    if (!D) return fail("NULL domain");
+    if (mode != 0 && mode != 1) return fail("halo mode is 0 (all populations) or 1 (inward populations)");
+    if (mode == D->halo_mode) return 0;
+    D->halo_mode = mode;
+    drop_graph(D);
+    return domain_build_plans(D);
 }
 
 int lbm_cu_domain_profile(lbm_domain *D, int enable) {

@@ -120,6 +120,33 @@ __device__ __forceinline__ int find_lattice(const LatDesc *tab, int ntab, int bl
     return lo;
 }
 
+// Arguments of a step launch.  Up to kParamLattices descriptors travel in
+// the kernel parameter space (constant bank: block-uniform values stay in
+// uniform registers); larger batches use a device table.
+constexpr int kParamLattices = 8;
+struct StepArgs {
+    LatDesc tab[kParamLattices];
+    const LatDesc *dtab;
+    int ntab;
+    int store_v, store_rho;
+};
+
+template <bool PT>
+__device__ __forceinline__ const LatDesc &lattice_of(const StepArgs &a) {
+    if (PT) {
+        int li = 0;
+        if (a.ntab > 1) {
+            int hi = a.ntab - 1;
+            while (li < hi) {
+                const int mid = (li + hi + 1) >> 1;
+                if (a.tab[mid].first_block <= (int)blockIdx.x) li = mid; else hi = mid - 1;
+            }
+        }
+        return a.tab[li];
+    }
+    return a.dtab[find_lattice(a.dtab, a.ntab, blockIdx.x)];
+}
+
 // ------------------------------------------------------------- equilibria
 // src/cl_programs/lbm_header.h:68-94
 template <typename R> __device__ __forceinline__ R eq_a0(R v, R v2, R r) {
@@ -155,32 +182,37 @@ __device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
 
 // BGK collision of a fluid cell; with LES the relaxation rate comes from the
 // Smagorinsky model of Hou, Sterling, Chen & Doolen (1996):
-//   tau_eff = (tau0 + sqrt(tau0^2 + C sqrt(Q))) / 2, Q = Pi:Pi,
-//   Pi_ab = sum_i e_ia e_ib (f_i - f_i^eq), C = 18 sqrt(2) Cs^2.
+//   tau_eff = (tau0 + sqrt(tau0^2 + C sqrt(Q))) / 2,  Q = Pi:Pi,  C = 18 sqrt(2) Cs^2,
+//   Pi_ab = sum_i e_ia e_ib f_i - rho/3 delta_ab - u_a u_b
+// (the second moment of the incompressible equilibrium is rho/3 delta + u u),
+// from the nine opposite-pair sums of the pre-collision populations.  rho is
+// the population sum, dp the equilibrium's dd_param.
 template <typename R, bool LES>
-__device__ __forceinline__ void collide(R f[19], R vx, R vy, R vz, R dp, const LatDesc &d) {
+__device__ __forceinline__ void collide(R f[19], R rho, R vx, R vy, R vz, R dp, const LatDesc &d) {
+    R w = par<R>(d, P_INV_TAU);
+    if (LES && par<R>(d, P_LES) != (R)0) {
+        R p[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) p[k] = f[2 * k] + f[2 * k + 1];
+        const R sxx = (((p[0] + p[2]) + p[3]) + p[4]) + p[5];
+        const R syy = (((p[1] + p[2]) + p[3]) + p[6]) + p[7];
+        const R szz = (((p[4] + p[5]) + p[6]) + p[7]) + p[8];
+        const R r3 = rho * K<R>::c3;
+        const R pxx = (sxx - r3) - vx * vx;
+        const R pyy = (syy - r3) - vy * vy;
+        const R pzz = (szz - r3) - vz * vz;
+        const R pxy = (p[2] - p[3]) - vx * vy;
+        const R pxz = (p[4] - p[5]) - vx * vz;
+        const R pyz = (p[6] - p[7]) - vy * vz;
+        const R q = ((pxx * pxx + pyy * pyy) + pzz * pzz) + (R)2 * ((pxy * pxy + pxz * pxz) + pyz * pyz);
+        const R tau0 = par<R>(d, P_TAU0);
+        const R te = (R)0.5 * (tau0 + dsqrt(tau0 * tau0 + par<R>(d, P_LES) * dsqrt(q)));
+        w = (R)1 / te;
+    }
     R eq[19];
     equilibria<R>(vx, vy, vz, dp, eq);
 #pragma unroll
-    for (int i = 0; i < 19; i++) eq[i] = eq[i] - f[i];
-    R w = par<R>(d, P_INV_TAU);
-    if (LES) {
-        R s[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) s[k] = eq[2 * k] + eq[2 * k + 1];
-        R pxx = (((s[0] + s[2]) + s[3]) + s[4]) + s[5];
-        R pyy = (((s[1] + s[2]) + s[3]) + s[6]) + s[7];
-        R pzz = (((s[4] + s[5]) + s[6]) + s[7]) + s[8];
-        R pxy = s[2] - s[3];
-        R pxz = s[4] - s[5];
-        R pyz = s[6] - s[7];
-        R q = ((pxx * pxx + pyy * pyy) + pzz * pzz) + (R)2 * ((pxy * pxy + pxz * pxz) + pyz * pyz);
-        R tau0 = par<R>(d, P_TAU0);
-        R te = (R)0.5 * (tau0 + dsqrt(tau0 * tau0 + par<R>(d, P_LES) * dsqrt(q)));
-        w = (R)1 / te;
-    }
-#pragma unroll
-    for (int i = 0; i < 19; i++) f[i] += w * eq[i];
+    for (int i = 0; i < 19; i++) f[i] += w * (eq[i] - f[i]);
 }
 
 // Gravity terms of the alpha kernel.  The reference aliases its temporary to
@@ -198,45 +230,44 @@ __device__ __forceinline__ R gravity_chain(R rho, const LatDesc &d, R t[9]) {
     return r;
 }
 
-// Index of the cell reached from c by the signed offset `off`, wrapped over
-// the whole buffer like the reference's DOMAIN_WRAP (src/cl_programs/wrap.h:
-// 112-127).  Only blocks near either end of the buffer need the wrap.
-__device__ __forceinline__ int64_t wrap_idx(int64_t c, int64_t off, int64_t n, bool wrap) {
-    int64_t i = c + off;
-    if (wrap) {
-        if (i < 0) i += n;
-        else if (i >= n) i -= n;
-    }
-    return i;
-}
-
 __device__ __forceinline__ int64_t dir_off(int i, int64_t nx, int64_t slice) {
     return (int64_t)dir_x(i) + (int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * slice;
 }
 
+// Cell reached from c by the signed offset `off`, wrapped over the whole
+// buffer like the reference's DOMAIN_WRAP (src/cl_programs/wrap.h:112-127).
+__device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) {
+    int64_t i = c + off;
+    if (i < 0) i += n;
+    else if (i >= n) i -= n;
+    return i;
+}
+
+// Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
+// registers) where the float kernels fit without spilling, fewer for double.
+template <typename S, bool LES, bool BETA>
+__host__ __device__ constexpr int min_blocks() {
+    return sizeof(typename Store<S>::R) == 8 ? 1 : (BETA || LES) ? 4 : 3;
+}
+
 // ------------------------------------------------------------------ beta
-template <typename S, bool LES>
-__global__ void __launch_bounds__(256) k_beta(const LatDesc *__restrict__ tab, int ntab, int store_v,
-                                              int store_rho) {
+// WRAP: the block holds cells within reach of either end of the buffer;
+// otherwise every neighbour address is the cell's address plus a
+// block-uniform offset.
+template <typename S, bool LES, bool WRAP>
+__device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store_v, int store_rho) {
     using R = typename Store<S>::R;
-    const int li = ntab == 1 ? 0 : find_lattice(tab, ntab, blockIdx.x);
-    const LatDesc &d = tab[li];
-    const int64_t n = d.n;
-    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
-    const int64_t c = c0 + threadIdx.x;
-    if (c >= n) return;
-    const int64_t nx = d.nx, slice = (int64_t)d.nx * d.ny;
-    const int64_t reach = nx + slice;
-    const bool wrap = (c0 < reach) || (c0 + (int64_t)blockDim.x - 1 + reach >= n);
-    S *dd = (S *)d.dd;
-    const int64_t ps = d.pstride;
+    S *const dd = (S *)d.dd;
+    S *const pc = dd + c;
+    const int64_t ps = d.pstride, nx = d.nx, sl = (int64_t)d.nx * d.ny, n = d.n;
     const int fl = d.flags[c];
 
     R f[19];
 #pragma unroll
     for (int i = 0; i < 19; i++) {
-        const int64_t src = wrap_idx(c, -dir_off(i, nx, slice), n, wrap);
-        f[i] = Store<S>::ld(dd + opp(i) * ps + src, weight<R>(i));
+        const int64_t off = dir_off(i, nx, sl);
+        const S *p = WRAP ? dd + opp(i) * ps + wrap_cell(c, -off, n) : pc + (opp(i) * ps - off);
+        f[i] = Store<S>::ld(p, weight<R>(i));
     }
     // moments in the order of lbm_beta.cl:261-483
     R r, vx, vy, vz;
@@ -262,8 +293,9 @@ __global__ void __launch_bounds__(256) k_beta(const LatDesc *__restrict__ tab, i
 
     if (fl == kFluid) {
         const R v2 = (vx * vx + vy * vy) + vz * vz;
-        r = r - K<R>::k15 * v2;  // dd_param aliases rho (lbm_beta.cl:493)
-        collide<R, LES>(f, vx, vy, vz, r, d);
+        const R dp = r - K<R>::k15 * v2;
+        collide<R, LES>(f, r, vx, vy, vz, dp, d);
+        r = dp;  // dd_param aliases rho (lbm_beta.cl:493)
     } else if (fl == kObstacle) {
         vx = 0; vy = 0; vz = 0;
 #pragma unroll
@@ -281,34 +313,46 @@ __global__ void __launch_bounds__(256) k_beta(const LatDesc *__restrict__ tab, i
     }
 #pragma unroll
     for (int i = 0; i < 19; i++) {
-        const int64_t dst = wrap_idx(c, dir_off(i, nx, slice), n, wrap);
-        Store<S>::st(dd + i * ps + dst, f[i], weight<R>(i));
+        const int64_t off = dir_off(i, nx, sl);
+        S *p = WRAP ? dd + i * ps + wrap_cell(c, off, n) : pc + (i * ps + off);
+        Store<S>::st(p, f[i], weight<R>(i));
     }
     if (fl == kGhost) return;
     if (store_v) {
-        R *u = (R *)d.vel;
-        u[c] = vx; u[d.n + c] = vy; u[2 * d.n + c] = vz;
+        R *u = (R *)d.vel + c;
+        u[0] = vx; u[n] = vy; u[2 * n] = vz;
     }
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_beta(const __grid_constant__ StepArgs a) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
+    const int64_t c = c0 + threadIdx.x;
+    if (c >= d.n) return;
+    const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny;
+    if (c0 < reach || c0 + (int64_t)blockDim.x - 1 + reach >= d.n)
+        beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+    else
+        beta_cell<S, LES, false>(d, c, a.store_v, a.store_rho);
+}
+
 // ----------------------------------------------------------------- alpha
-template <typename S, bool LES>
-__global__ void __launch_bounds__(256) k_alpha(const LatDesc *__restrict__ tab, int ntab, int store_v,
-                                               int store_rho) {
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ StepArgs a) {
     using R = typename Store<S>::R;
-    const int li = ntab == 1 ? 0 : find_lattice(tab, ntab, blockIdx.x);
-    const LatDesc &d = tab[li];
+    const LatDesc &d = lattice_of<PT>(a);
     const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     const int fl = d.flags[c];
     if (fl == kGhost) return;  // lbm_alpha.cl:31-32
-    S *dd = (S *)d.dd;
+    S *const pc = (S *)d.dd + c;
     const int64_t ps = d.pstride;
 
     R f[19];
 #pragma unroll
-    for (int i = 0; i < 19; i++) f[i] = Store<S>::ld(dd + i * ps + c, weight<R>(i));
+    for (int i = 0; i < 19; i++) f[i] = Store<S>::ld(pc + i * ps, weight<R>(i));
     // moments in the order of lbm_alpha.cl:61-156
     R r, vx, vy, vz;
     r = f[0]; vx = f[0];
@@ -336,7 +380,7 @@ __global__ void __launch_bounds__(256) k_alpha(const LatDesc *__restrict__ tab, 
     if (fl == kFluid) {
         const R v2 = (vx * vx + vy * vy) + vz * vz;
         const R dp = r - K<R>::k15 * v2;
-        collide<R, LES>(f, vx, vy, vz, dp, d);
+        collide<R, LES>(f, r, vx, vy, vz, dp, d);
         r = gravity_chain<R>(r, d, t);
         write = true;
     } else if (fl == kObstacle) {
@@ -360,13 +404,13 @@ __global__ void __launch_bounds__(256) k_alpha(const LatDesc *__restrict__ tab, 
         }
         // each population goes to the opposite slot (lbm_alpha.cl:185-301)
 #pragma unroll
-        for (int i = 0; i < 19; i++) Store<S>::st(dd + opp(i) * ps + c, f[i], weight<R>(i));
+        for (int i = 0; i < 19; i++) Store<S>::st(pc + opp(i) * ps, f[i], weight<R>(i));
     }
-    if (store_v) {
-        R *u = (R *)d.vel;
-        u[c] = vx; u[d.n + c] = vy; u[2 * d.n + c] = vz;
+    if (a.store_v) {
+        R *u = (R *)d.vel + c;
+        u[0] = vx; u[d.n] = vy; u[2 * d.n] = vz;
     }
-    if (store_rho) ((R *)d.rho)[c] = r;
+    if (a.store_rho) ((R *)d.rho)[c] = r;
 }
 
 }  // namespace lbm
