@@ -102,6 +102,15 @@ int lbm_cu_perturb(lbm_lattice *lat, const int origin[3], const int phys[3], uin
  * CLbmSolver::simulationStep (src/CLbmSolver.hpp:664-676). */
 int lbm_cu_step(lbm_lattice *lat, int parity, void *stream);
 
+/* Kernel shape of the step: 1 (default) is one cell per thread; 2 processes
+ * two neighbouring x cells per thread with 64-bit accesses (32-bit for 16-bit
+ * storage) where the arithmetic type is float and nx is even, else falls back
+ * to 1.  Both shapes give bit-identical results; on GB300 the one-cell shape
+ * is faster for the sizes measured (more resident warps).  No reference counterpart (the
+ * reference's work-group size list, src/CLbmSolver.hpp:279-312, tunes its
+ * OpenCL launch instead). */
+int lbm_cu_set_kernel_shape(lbm_lattice *lat, int cells_per_thread);
+
 /* Rectangular copy of one field between the lattice and a HOST buffer laid
  * out [plane][z][y][x] of size[0]*size[1]*size[2] cells per plane, elements
  * of the arithmetic type (float for F32/F16/BF16, double for F64) or int32
@@ -164,6 +173,8 @@ int lbm_cu_domain_set_store_interval(lbm_domain *dom, int interval);
  * Both give identical fluid, lid and wall cells; ghost-layer populations
  * differ in the 14 slots no other cell reads. */
 int lbm_cu_domain_set_halo_mode(lbm_domain *dom, int mode);
+/* Kernel shape of every subdomain's step (see lbm_cu_set_kernel_shape). */
+int lbm_cu_domain_set_kernel_shape(lbm_domain *dom, int cells_per_thread);
 /* Time every step-kernel launch with a pair of CUDA events on the launching
  * stream (steps then run without graph replay), and read the accumulated
  * milliseconds and launch count (reset != 0 clears them).  Stands in for the

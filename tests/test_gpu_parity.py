@@ -70,12 +70,15 @@ def test_init_matches_oracle(capi, oracle_mod, storage):
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
 @pytest.mark.parametrize("cs", [0.0, 0.17])
 @pytest.mark.parametrize("gravity", [(0.0, 0.0, 0.0), (1e-5, -2e-5, 3e-6)])
-def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity):
-    """Perturbed lid cavity with odd sizes: every array, every step."""
+@pytest.mark.parametrize("dims,shape", [((21, 14, 11), 1), ((22, 14, 11), 2), ((64, 12, 18), 2)])
+def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity, dims, shape):
+    """Perturbed lid cavity: every array, every step, for the one-cell and
+    the two-cell kernel shapes (the latter needs an even x extent; the 64-wide
+    case has whole warps inside the lattice)."""
     api, O = capi, oracle_mod
-    dims = (21, 14, 11)
     p = oracle_params(O, storage, dims, cs, gravity)
     L = gpu_single(api, O, dims, storage, p, perturb=(SEED, 2e-2))
+    L.set_kernel_shape(shape)
     s = O.single(O.OracleKernels(storage), dims, p, storage)
     s.k.perturb(s.lat, (0, 0, 0), dims, SEED, 2e-2)
     compare(api, O, L, s, storage, "after start-up")
@@ -105,8 +108,8 @@ def test_matches_reference_arrays(capi, oracle_mod, storage):
             assert n_diff(rho, g[f"rho{k}"]) == 0, f"step {k}"
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64"])
-def test_c1_matches_reference_every_step(capi, oracle_mod, storage):
+@pytest.mark.parametrize("storage,shape", [("f32", 1), ("f32", 2), ("f64", 1)])
+def test_c1_matches_reference_every_step(capi, oracle_mod, storage, shape):
     """Config 1 geometry (64^3 lid cavity, Re 1000, U 0.05, rest start) with
     the reference's plain BGK: the state hash equals the reference kernels'
     after every step (100 steps f32, 40 f64)."""
@@ -116,6 +119,7 @@ def test_c1_matches_reference_every_step(capi, oracle_mod, storage):
     rdt = O.STORAGE[storage][1]
     p = O.Params.lattice(O.cavity_tau(0.05, 64, 1000.0), 0.05, dtype=rdt)
     L = gpu_single(api, O, dims, storage, p)
+    L.set_kernel_shape(shape)
     flags = L.read(api.FIELD_FLAGS)[0]
     m = O.fluid_mask(flags)
 
@@ -143,8 +147,8 @@ def test_c1_smagorinsky_matches_oracle(capi, oracle_mod):
         compare(api, O, L, s, "f32", f"after step {k + 1}")
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
-def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph):
+@pytest.mark.parametrize("use_graph,shape", [(False, 1), (True, 1), (True, 2)])
+def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph, shape):
     """2x2x1 decomposition on one GPU: every subdomain's state hash equals the
     reference kernels' with the reference host exchange, every step."""
     api, O = capi, oracle_mod
@@ -152,6 +156,7 @@ def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph):
     p = O.Params.lattice(O.cavity_tau(0.1, 22, 1000.0), 0.1, dtype=np.float32)
     D = api.Domain((24, 16, 16), (2, 2, 1), api.F32, True, True)
     D.set_params(gpu_params(api, p))
+    D.set_kernel_shape(shape)
     D.reset()
     D.perturb(SEED, 1e-2)
     done = 0

@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
         "lbm_cu_init": ([vp, ip, vp], ci),
         "lbm_cu_perturb": ([vp, ip, ip, u64, cd, vp], ci),
         "lbm_cu_step": ([vp, ci, vp], ci),
+        "lbm_cu_set_kernel_shape": ([vp, ci], ci),
         "lbm_cu_read": ([vp, ci, ip, ip, vp, vp], ci),
         "lbm_cu_write": ([vp, ci, ip, ip, vp, ip, vp], ci),
         "lbm_cu_halo": ([vp, ip, vp, ip, ip, ip, vp], ci),
@@ -81,6 +82,7 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_counter": ([vp, C.POINTER(i64)], ci),
         "lbm_cu_domain_set_store_interval": ([vp, ci], ci),
         "lbm_cu_domain_set_halo_mode": ([vp, ci], ci),
+        "lbm_cu_domain_set_kernel_shape": ([vp, ci], ci),
         "lbm_cu_domain_profile": ([vp, ci], ci),
         "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
@@ -150,6 +152,9 @@ class Lattice:
 
     def step(self, parity: int, stream=None):
         check(lib().lbm_cu_step(self.h, parity, stream))
+
+    def set_kernel_shape(self, cells_per_thread: int):
+        check(lib().lbm_cu_set_kernel_shape(self.h, cells_per_thread))
 
     def _shape(self, field, size):
         sx, sy, sz = size
@@ -238,6 +243,9 @@ class Domain:
 
     def set_store_interval(self, interval: int):
         check(lib().lbm_cu_domain_set_store_interval(self.h, interval))
+
+    def set_kernel_shape(self, cells_per_thread: int):
+        check(lib().lbm_cu_domain_set_kernel_shape(self.h, cells_per_thread))
 
     def set_halo_mode(self, mode: int):
         """0: all 19 populations after alpha (reference); 1: the 5 read inward."""

@@ -58,6 +58,7 @@ struct lbm_lattice {
     bool dirty = true;
     void *stage = nullptr;  // staging for host copies and reduction partials
     size_t stage_bytes = 0;
+    bool allow_pair = false;  // two-cell kernels where the shape allows (tuning option)
 };
 
 namespace {
@@ -372,27 +373,46 @@ __global__ void k_reduce_final(const double *partial, int nblocks, double *out) 
 }
 
 // ------------------------------------------------------------- dispatchers
-template <typename S>
+template <typename S, bool PAIR>
 int launch_step_t(int parity, bool les, const StepArgs &a, int blocks, cudaStream_t st) {
     if (blocks <= 0) return 0;
     const bool pt = a.ntab <= kParamLattices;
 #define STEP(K_, L_, P_) K_<S, L_, P_><<<blocks, kBlock, 0, st>>>(a)
-    if (parity) {
-        if (les) { if (pt) STEP(k_alpha, true, true); else STEP(k_alpha, true, false); }
-        else { if (pt) STEP(k_alpha, false, true); else STEP(k_alpha, false, false); }
-    } else {
-        if (les) { if (pt) STEP(k_beta, true, true); else STEP(k_beta, true, false); }
-        else { if (pt) STEP(k_beta, false, true); else STEP(k_beta, false, false); }
+#define STEPS(KA_, KB_)                                                                   \
+    if (parity) {                                                                         \
+        if (les) { if (pt) STEP(KA_, true, true); else STEP(KA_, true, false); }          \
+        else { if (pt) STEP(KA_, false, true); else STEP(KA_, false, false); }            \
+    } else {                                                                              \
+        if (les) { if (pt) STEP(KB_, true, true); else STEP(KB_, true, false); }          \
+        else { if (pt) STEP(KB_, false, true); else STEP(KB_, false, false); }            \
     }
+    if constexpr (PAIR) {
+        STEPS(k_alpha2, k_beta2)
+    } else {
+        STEPS(k_alpha, k_beta)
+    }
+#undef STEPS
 #undef STEP
     CU(cudaGetLastError());
     return 0;
 }
 
-// One step over `ntab` lattices: descriptors from the host copy `htab`
-// (kernel parameters when they fit), else from the device table `dtab`.
-int launch_step(int storage, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab, int blocks,
-                int sv, int sr, cudaStream_t st) {
+// The two-cell kernels apply to the float arithmetic types when every
+// lattice of the launch has an even x extent.
+bool pair_shape(int storage, const LatDesc *tab, int ntab) {
+    if (storage == kF64) return false;
+    for (int i = 0; i < ntab; i++)
+        if (tab[i].nx & 1) return false;
+    return true;
+}
+
+int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
+
+// One step over `ntab` lattices.  `htab` holds the host copy of the
+// descriptors with first_block/nblocks for the launch shape; the launch uses
+// it as kernel parameters when it fits, else the device copy `dtab`.
+int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab,
+                int blocks, int sv, int sr, cudaStream_t st) {
     StepArgs a;
     memset(&a, 0, sizeof(a));
     a.ntab = ntab;
@@ -401,11 +421,19 @@ int launch_step(int storage, int parity, bool les, const LatDesc *htab, const La
     a.store_rho = sr;
     if (ntab <= kParamLattices)
         for (int i = 0; i < ntab; i++) a.tab[i] = htab[i];
+    if (pair) {
+        switch (storage) {
+            case kF32: return launch_step_t<float, true>(parity, les, a, blocks, st);
+            case kF16: return launch_step_t<__half, true>(parity, les, a, blocks, st);
+            case kBF16: return launch_step_t<__nv_bfloat16, true>(parity, les, a, blocks, st);
+        }
+        return fail("the two-cell kernels need a float arithmetic type");
+    }
     switch (storage) {
-        case kF32: return launch_step_t<float>(parity, les, a, blocks, st);
-        case kF64: return launch_step_t<double>(parity, les, a, blocks, st);
-        case kF16: return launch_step_t<__half>(parity, les, a, blocks, st);
-        case kBF16: return launch_step_t<__nv_bfloat16>(parity, les, a, blocks, st);
+        case kF32: return launch_step_t<float, false>(parity, les, a, blocks, st);
+        case kF64: return launch_step_t<double, false>(parity, les, a, blocks, st);
+        case kF16: return launch_step_t<__half, false>(parity, les, a, blocks, st);
+        case kBF16: return launch_step_t<__nv_bfloat16, false>(parity, les, a, blocks, st);
     }
     return fail("unknown storage type");
 }
@@ -573,8 +601,12 @@ int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t see
 
 int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
     if (!l) return fail("NULL lattice");
-    return launch_step(l->storage, parity & 1, uses_les(l->h), &l->h, nullptr, 1, l->h.nblocks, l->store_v,
-                       l->store_rho, S(stream));
+    LatDesc h = l->h;
+    const bool pair = l->allow_pair && pair_shape(l->storage, &h, 1);
+    h.first_block = 0;
+    h.nblocks = (int)((l->n + cells_per_block(pair) - 1) / cells_per_block(pair));
+    return launch_step(l->storage, pair, parity & 1, uses_les(h), &h, nullptr, 1, h.nblocks, l->store_v, l->store_rho,
+                       S(stream));
 }
 
 static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], void *host, const int norm[3],
@@ -720,9 +752,10 @@ struct lbm_domain {
     std::vector<std::vector<CommGeom>> comms;
     std::vector<std::vector<int>> bc;
     std::vector<int> coords;  // 3 per subdomain
-    LatDesc *d_tab = nullptr;
-    std::vector<LatDesc> h_tab;
-    int blocks = 0;
+    LatDesc *d_tab[2] = {nullptr, nullptr};  // [one-cell, two-cell] block numbering
+    std::vector<LatDesc> h_tab[2];
+    int blocks[2] = {0, 0};
+    bool pair = false;
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
     std::vector<HaloDesc> plan[2][3];
@@ -730,6 +763,7 @@ struct lbm_domain {
     int64_t plan_cells[2][3] = {};
     int plan_planes[2][3] = {};
     int halo_mode = 0;  // 0: all 19 populations after alpha (reference), 1: the 5 read inward
+    bool allow_pair = false;
     int64_t counter = 0;
     int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
     cudaGraphExec_t graph = nullptr;
@@ -796,17 +830,22 @@ int domain_build_plans(lbm_domain *D) {
 
 int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
     if (!D->tab_dirty) return 0;
-    std::vector<LatDesc> tab;
-    int first = 0;
-    for (auto *l : D->subs) {
-        LatDesc h = l->h;
-        h.first_block = first;
-        first += h.nblocks;
-        tab.push_back(h);
+    for (int shape = 0; shape < 2; shape++) {
+        std::vector<LatDesc> tab;
+        int first = 0;
+        const int per = cells_per_block(shape == 1);
+        for (auto *l : D->subs) {
+            LatDesc h = l->h;
+            h.first_block = first;
+            h.nblocks = (int)((l->n + per - 1) / per);
+            first += h.nblocks;
+            tab.push_back(h);
+        }
+        D->blocks[shape] = first;
+        D->h_tab[shape] = tab;
+        CU(cudaMemcpyAsync(D->d_tab[shape], tab.data(), tab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice, st));
     }
-    D->blocks = first;
-    D->h_tab = tab;
-    CU(cudaMemcpyAsync(D->d_tab, tab.data(), tab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice, st));
+    D->pair = D->allow_pair && pair_shape(D->storage, D->h_tab[1].data(), (int)D->subs.size());
     CU(cudaStreamSynchronize(st));
     D->tab_dirty = false;
     return 0;
@@ -828,7 +867,9 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
     const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (timed && domain_record(D, st, &e0)) return -1;
-    if (launch_step(D->storage, parity, les, D->h_tab.data(), D->d_tab, (int)D->subs.size(), D->blocks, sv, sr, st))
+    const int sh = D->pair ? 1 : 0;
+    if (launch_step(D->storage, D->pair, parity, les, D->h_tab[sh].data(), D->d_tab[sh], (int)D->subs.size(),
+                    D->blocks[sh], sv, sr, st))
         return -1;
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
@@ -901,10 +942,11 @@ int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int 
         D->bc.push_back(bc);
         D->comms.push_back(cms);
     }
-    if (cudaMalloc((void **)&D->d_tab, nsub * sizeof(LatDesc)) != cudaSuccess) {
-        lbm_cu_domain_destroy(D);
-        return fail("cudaMalloc of the subdomain table failed");
-    }
+    for (int shape = 0; shape < 2; shape++)
+        if (cudaMalloc((void **)&D->d_tab[shape], nsub * sizeof(LatDesc)) != cudaSuccess) {
+            lbm_cu_domain_destroy(D);
+            return fail("cudaMalloc of the subdomain table failed");
+        }
     if (domain_build_plans(D)) {
         std::string m = g_err;
         lbm_cu_domain_destroy(D);
@@ -920,7 +962,8 @@ int lbm_cu_domain_destroy(lbm_domain *D) {
     if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
     for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
     for (auto *l : D->subs) lbm_cu_destroy(l);
-    if (D->d_tab) cudaFree(D->d_tab);
+    for (int shape = 0; shape < 2; shape++)
+        if (D->d_tab[shape]) cudaFree(D->d_tab[shape]);
     for (int p = 0; p < 2; p++)
         for (int a = 0; a < 3; a++)
             if (D->d_plan[p][a]) cudaFree(D->d_plan[p][a]);
@@ -1023,6 +1066,22 @@ int lbm_cu_domain_set_store_interval(lbm_domain *D, int interval) {
     if (!D) return fail("NULL domain");
     if (interval < 0) return fail("negative store interval");
     D->store_interval = interval;
+    return 0;
+}
+
+int lbm_cu_set_kernel_shape(lbm_lattice *l, int cells_per_thread) {
+    if (!l) return fail("NULL lattice");
+    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
+    l->allow_pair = cells_per_thread == 2;
+    return 0;
+}
+
+int lbm_cu_domain_set_kernel_shape(lbm_domain *D, int cells_per_thread) {
+    if (!D) return fail("NULL domain");
+    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
+    D->allow_pair = cells_per_thread == 2;
+    D->tab_dirty = true;
+    drop_graph(D);
     return 0;
 }
 

@@ -17,6 +17,13 @@
 // is compiled with -fmad=false and IEEE division/square root, which makes the
 // results bit-identical to the reference kernel source run on a CPU.
 //
+// Two kernel shapes:
+//   k_beta / k_alpha    one cell per thread, any storage and size;
+//   k_beta2 / k_alpha2  two neighbouring x cells per thread for the float
+//                       arithmetic types and even nx: 64-bit loads/stores
+//                       (32-bit for the 16-bit storage types), pairwise
+//                       IEEE arithmetic, warp shuffles for the populations
+//                       that move along x.
 // Population storage: float, double, or the shifted half / bfloat16 forms
 // that store f_i - w_i and compute in float.
 #pragma once
@@ -45,31 +52,79 @@ __host__ __device__ constexpr int dir_z(int i) {
 }
 __host__ __device__ constexpr int opp(int i) { return i == 18 ? 18 : (i ^ 1); }
 
+// ------------------------------------------------------ float pairs
+// Two float lanes (two cells).  Every lane is one IEEE round-to-nearest
+// operation (__fadd_rn/__fsub_rn/__fmul_rn are never contracted into a
+// multiply-add), so a pair computes exactly what two scalar cells compute.
+// The packed f32x2 PTX forms were measured to differ from the scalar result
+// by up to 5 ulp in this kernel, so they are not used.
+struct P2 {
+    float x, y;
+};
+__device__ __forceinline__ P2 operator+(P2 a, P2 b) { return P2{__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)}; }
+__device__ __forceinline__ P2 operator-(P2 a, P2 b) { return P2{__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)}; }
+__device__ __forceinline__ P2 operator*(P2 a, P2 b) { return P2{__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)}; }
+__device__ __forceinline__ P2 operator-(P2 a) { return P2{-a.x, -a.y}; }
+__device__ __forceinline__ P2 &operator+=(P2 &a, P2 b) { return a = a + b; }
+__device__ __forceinline__ P2 &operator-=(P2 &a, P2 b) { return a = a - b; }
+
+// broadcast of a scalar to the math type
+template <typename M> struct Bc;
+template <> struct Bc<float> { __device__ static __forceinline__ float of(float v) { return v; } };
+template <> struct Bc<double> { __device__ static __forceinline__ double of(double v) { return v; } };
+template <> struct Bc<P2> { __device__ static __forceinline__ P2 of(float v) { return P2{v, v}; } };
+template <typename M> struct Scalar { using T = M; };
+template <> struct Scalar<P2> { using T = float; };
+
+__device__ __forceinline__ float msqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ P2 msqrt(P2 x) { return P2{sqrtf(x.x), sqrtf(x.y)}; }
+__device__ __forceinline__ float mrcp(float x) { return 1.0f / x; }
+__device__ __forceinline__ double mrcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ P2 mrcp(P2 x) { return P2{1.0f / x.x, 1.0f / x.y}; }
+
 // ---------------------------------------------------------------- storage
 template <typename S> struct Store;
 template <> struct Store<float> {
     using R = float;
-    static constexpr bool kShifted = false;
     __device__ static __forceinline__ R ld(const float *p, R) { return *p; }
     __device__ static __forceinline__ void st(float *p, R v, R) { *p = v; }
+    __device__ static __forceinline__ P2 ld2(const float *p, R) {
+        const float2 v = *(const float2 *)p;
+        return P2{v.x, v.y};
+    }
+    __device__ static __forceinline__ void st2(float *p, P2 v, R) { *(float2 *)p = make_float2(v.x, v.y); }
 };
 template <> struct Store<double> {
     using R = double;
-    static constexpr bool kShifted = false;
     __device__ static __forceinline__ R ld(const double *p, R) { return *p; }
     __device__ static __forceinline__ void st(double *p, R v, R) { *p = v; }
 };
 template <> struct Store<__half> {
     using R = float;
-    static constexpr bool kShifted = true;
     __device__ static __forceinline__ R ld(const __half *p, R w) { return __half2float(*p) + w; }
     __device__ static __forceinline__ void st(__half *p, R v, R w) { *p = __float2half_rn(v - w); }
+    __device__ static __forceinline__ P2 ld2(const __half *p, R w) {
+        const float2 v = __half22float2(*(const __half2 *)p);
+        return P2{v.x, v.y} + P2{w, w};
+    }
+    __device__ static __forceinline__ void st2(__half *p, P2 v, R w) {
+        const P2 t = v - P2{w, w};
+        *(__half2 *)p = __floats2half2_rn(t.x, t.y);
+    }
 };
 template <> struct Store<__nv_bfloat16> {
     using R = float;
-    static constexpr bool kShifted = true;
     __device__ static __forceinline__ R ld(const __nv_bfloat16 *p, R w) { return __bfloat162float(*p) + w; }
     __device__ static __forceinline__ void st(__nv_bfloat16 *p, R v, R w) { *p = __float2bfloat16_rn(v - w); }
+    __device__ static __forceinline__ P2 ld2(const __nv_bfloat16 *p, R w) {
+        const float2 v = __bfloat1622float2(*(const __nv_bfloat162 *)p);
+        return P2{v.x, v.y} + P2{w, w};
+    }
+    __device__ static __forceinline__ void st2(__nv_bfloat16 *p, P2 v, R w) {
+        const P2 t = v - P2{w, w};
+        *(__nv_bfloat162 *)p = __floats2bfloat162_rn(t.x, t.y);
+    }
 };
 
 // Constants exactly as the reference writes them: (T)(float literal).
@@ -99,9 +154,9 @@ struct LatDesc {
     int64_t n;         // cells
     int32_t nx, ny, nz;
     int32_t first_block;  // first block of this lattice in a batched launch
-    int32_t nblocks;
-    int32_t grav;      // gravity chain non-zero (alpha kernel)
-    double pd[16];     // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
+    int32_t nblocks;      // blocks of the launched kernel shape
+    int32_t grav;         // gravity chain non-zero (alpha kernel)
+    double pd[16];        // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
     float pf[16];
 };
 enum { P_INV_TAU = 0, P_TAU0 = 1, P_LES = 2, P_LID = 3, P_K0 = 4 };
@@ -109,6 +164,9 @@ enum { P_INV_TAU = 0, P_TAU0 = 1, P_LES = 2, P_LID = 3, P_K0 = 4 };
 template <typename R> __device__ __forceinline__ R par(const LatDesc &d, int i);
 template <> __device__ __forceinline__ float par<float>(const LatDesc &d, int i) { return d.pf[i]; }
 template <> __device__ __forceinline__ double par<double>(const LatDesc &d, int i) { return d.pd[i]; }
+template <typename M> __device__ __forceinline__ M parm(const LatDesc &d, int i) {
+    return Bc<M>::of(par<typename Scalar<M>::T>(d, i));
+}
 
 // Lattice of a block in a batched launch: binary search on first_block.
 __device__ __forceinline__ int find_lattice(const LatDesc *tab, int ntab, int block) {
@@ -122,7 +180,8 @@ __device__ __forceinline__ int find_lattice(const LatDesc *tab, int ntab, int bl
 
 // Arguments of a step launch.  Up to kParamLattices descriptors travel in
 // the kernel parameter space (constant bank: block-uniform values stay in
-// uniform registers); larger batches use a device table.
+// uniform registers); larger batches use a device table.  first_block and
+// nblocks count blocks of the launched kernel shape.
 constexpr int kParamLattices = 8;
 struct StepArgs {
     LatDesc tab[kParamLattices];
@@ -148,23 +207,28 @@ __device__ __forceinline__ const LatDesc &lattice_of(const StepArgs &a) {
 }
 
 // ------------------------------------------------------------- equilibria
-// src/cl_programs/lbm_header.h:68-94
-template <typename R> __device__ __forceinline__ R eq_a0(R v, R v2, R r) {
-    return K<R>::c18 * ((r + K<R>::k3 * v) + K<R>::k45 * v2);
+// src/cl_programs/lbm_header.h:68-94, for a scalar or a packed pair M.
+template <typename M> __device__ __forceinline__ M eq_a0(M v, M v2, M r) {
+    using R = typename Scalar<M>::T;
+    return Bc<M>::of(K<R>::c18) * ((r + Bc<M>::of(K<R>::k3) * v) + Bc<M>::of(K<R>::k45) * v2);
 }
-template <typename R> __device__ __forceinline__ R eq_a1(R v, R v2, R r) {
-    return K<R>::c18 * ((r + K<R>::km3 * v) + K<R>::k45 * v2);
+template <typename M> __device__ __forceinline__ M eq_a1(M v, M v2, M r) {
+    using R = typename Scalar<M>::T;
+    return Bc<M>::of(K<R>::c18) * ((r + Bc<M>::of(K<R>::km3) * v) + Bc<M>::of(K<R>::k45) * v2);
 }
-template <typename R> __device__ __forceinline__ R eq_d4(R s, R s2, R r) {
-    return K<R>::c36 * ((r + K<R>::k3 * s) + K<R>::k45 * s2);
+template <typename M> __device__ __forceinline__ M eq_d4(M s, M s2, M r) {
+    using R = typename Scalar<M>::T;
+    return Bc<M>::of(K<R>::c36) * ((r + Bc<M>::of(K<R>::k3) * s) + Bc<M>::of(K<R>::k45) * s2);
 }
-template <typename R> __device__ __forceinline__ R eq_d5(R s, R s2, R r) {
-    return K<R>::c36 * ((r + K<R>::km3 * s) + K<R>::k45 * s2);
+template <typename M> __device__ __forceinline__ M eq_d5(M s, M s2, M r) {
+    using R = typename Scalar<M>::T;
+    return Bc<M>::of(K<R>::c36) * ((r + Bc<M>::of(K<R>::km3) * s) + Bc<M>::of(K<R>::k45) * s2);
 }
 
-template <typename R>
-__device__ __forceinline__ void equilibria(R vx, R vy, R vz, R dp, R eq[19]) {
-    R v2, s;
+template <typename M>
+__device__ __forceinline__ void equilibria(M vx, M vy, M vz, M dp, M eq[19]) {
+    using R = typename Scalar<M>::T;
+    M v2, s;
     v2 = vx * vx; eq[0] = eq_a0(vx, v2, dp); eq[1] = eq_a1(vx, v2, dp);
     v2 = vy * vy; eq[2] = eq_a0(vy, v2, dp); eq[3] = eq_a1(vy, v2, dp);
     s = vx + vy; v2 = s * s; eq[4] = eq_d4(s, v2, dp); eq[5] = eq_d5(s, v2, dp);
@@ -174,11 +238,8 @@ __device__ __forceinline__ void equilibria(R vx, R vy, R vz, R dp, R eq[19]) {
     s = vy + vz; v2 = s * s; eq[12] = eq_d4(s, v2, dp); eq[13] = eq_d5(s, v2, dp);
     s = vy - vz; v2 = s * s; eq[14] = eq_d4(s, v2, dp); eq[15] = eq_d5(s, v2, dp);
     v2 = vz * vz; eq[16] = eq_a0(vz, v2, dp); eq[17] = eq_a1(vz, v2, dp);
-    eq[18] = K<R>::c3 * dp;
+    eq[18] = Bc<M>::of(K<R>::c3) * dp;
 }
-
-__device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
-__device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
 
 // BGK collision of a fluid cell; with LES the relaxation rate comes from the
 // Smagorinsky model of Hou, Sterling, Chen & Doolen (1996):
@@ -187,30 +248,31 @@ __device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
 // (the second moment of the incompressible equilibrium is rho/3 delta + u u),
 // from the nine opposite-pair sums of the pre-collision populations.  rho is
 // the population sum, dp the equilibrium's dd_param.
-template <typename R, bool LES>
-__device__ __forceinline__ void collide(R f[19], R rho, R vx, R vy, R vz, R dp, const LatDesc &d) {
-    R w = par<R>(d, P_INV_TAU);
+template <typename M, bool LES>
+__device__ __forceinline__ void collide(M f[19], M rho, M vx, M vy, M vz, M dp, const LatDesc &d) {
+    using R = typename Scalar<M>::T;
+    M w = parm<M>(d, P_INV_TAU);
     if (LES && par<R>(d, P_LES) != (R)0) {
-        R p[9];
+        M p[9];
 #pragma unroll
         for (int k = 0; k < 9; k++) p[k] = f[2 * k] + f[2 * k + 1];
-        const R sxx = (((p[0] + p[2]) + p[3]) + p[4]) + p[5];
-        const R syy = (((p[1] + p[2]) + p[3]) + p[6]) + p[7];
-        const R szz = (((p[4] + p[5]) + p[6]) + p[7]) + p[8];
-        const R r3 = rho * K<R>::c3;
-        const R pxx = (sxx - r3) - vx * vx;
-        const R pyy = (syy - r3) - vy * vy;
-        const R pzz = (szz - r3) - vz * vz;
-        const R pxy = (p[2] - p[3]) - vx * vy;
-        const R pxz = (p[4] - p[5]) - vx * vz;
-        const R pyz = (p[6] - p[7]) - vy * vz;
-        const R q = ((pxx * pxx + pyy * pyy) + pzz * pzz) + (R)2 * ((pxy * pxy + pxz * pxz) + pyz * pyz);
-        const R tau0 = par<R>(d, P_TAU0);
-        const R te = (R)0.5 * (tau0 + dsqrt(tau0 * tau0 + par<R>(d, P_LES) * dsqrt(q)));
-        w = (R)1 / te;
+        const M sxx = (((p[0] + p[2]) + p[3]) + p[4]) + p[5];
+        const M syy = (((p[1] + p[2]) + p[3]) + p[6]) + p[7];
+        const M szz = (((p[4] + p[5]) + p[6]) + p[7]) + p[8];
+        const M r3 = rho * Bc<M>::of(K<R>::c3);
+        const M pxx = (sxx - r3) - vx * vx;
+        const M pyy = (syy - r3) - vy * vy;
+        const M pzz = (szz - r3) - vz * vz;
+        const M pxy = (p[2] - p[3]) - vx * vy;
+        const M pxz = (p[4] - p[5]) - vx * vz;
+        const M pyz = (p[6] - p[7]) - vy * vz;
+        const M q = ((pxx * pxx + pyy * pyy) + pzz * pzz) + Bc<M>::of((R)2) * ((pxy * pxy + pxz * pxz) + pyz * pyz);
+        const M tau0 = parm<M>(d, P_TAU0);
+        const M te = Bc<M>::of((R)0.5) * (tau0 + msqrt(tau0 * tau0 + parm<M>(d, P_LES) * msqrt(q)));
+        w = mrcp(te);
     }
-    R eq[19];
-    equilibria<R>(vx, vy, vz, dp, eq);
+    M eq[19];
+    equilibria<M>(vx, vy, vz, dp, eq);
 #pragma unroll
     for (int i = 0; i < 19; i++) f[i] += w * (eq[i] - f[i]);
 }
@@ -219,58 +281,21 @@ __device__ __forceinline__ void collide(R f[19], R rho, R vx, R vy, R vz, R dp, 
 // rho (lbm_alpha.cl:173): term k is coefficient k times term k-1, and the
 // stored density is the last term.  Coefficients k0..k8 come pre-multiplied
 // from the host.
-template <typename R>
-__device__ __forceinline__ R gravity_chain(R rho, const LatDesc &d, R t[9]) {
-    R r = rho;
+template <typename M>
+__device__ __forceinline__ M gravity_chain(M rho, const LatDesc &d, M t[9]) {
+    M r = rho;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
-        r = par<R>(d, P_K0 + k) * r;
+        r = parm<M>(d, P_K0 + k) * r;
         t[k] = r;
     }
     return r;
 }
 
-__device__ __forceinline__ int64_t dir_off(int i, int64_t nx, int64_t slice) {
-    return (int64_t)dir_x(i) + (int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * slice;
-}
-
-// Cell reached from c by the signed offset `off`, wrapped over the whole
-// buffer like the reference's DOMAIN_WRAP (src/cl_programs/wrap.h:112-127).
-__device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) {
-    int64_t i = c + off;
-    if (i < 0) i += n;
-    else if (i >= n) i -= n;
-    return i;
-}
-
-// Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
-// registers) where the float kernels fit without spilling, fewer for double.
-template <typename S, bool LES, bool BETA>
-__host__ __device__ constexpr int min_blocks() {
-    return sizeof(typename Store<S>::R) == 8 ? 1 : (BETA || LES) ? 4 : 3;
-}
-
-// ------------------------------------------------------------------ beta
-// WRAP: the block holds cells within reach of either end of the buffer;
-// otherwise every neighbour address is the cell's address plus a
-// block-uniform offset.
-template <typename S, bool LES, bool WRAP>
-__device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store_v, int store_rho) {
-    using R = typename Store<S>::R;
-    S *const dd = (S *)d.dd;
-    S *const pc = dd + c;
-    const int64_t ps = d.pstride, nx = d.nx, sl = (int64_t)d.nx * d.ny, n = d.n;
-    const int fl = d.flags[c];
-
-    R f[19];
-#pragma unroll
-    for (int i = 0; i < 19; i++) {
-        const int64_t off = dir_off(i, nx, sl);
-        const S *p = WRAP ? dd + opp(i) * ps + wrap_cell(c, -off, n) : pc + (opp(i) * ps - off);
-        f[i] = Store<S>::ld(p, weight<R>(i));
-    }
-    // moments in the order of lbm_beta.cl:261-483
-    R r, vx, vy, vz;
+// Moments in the order of lbm_beta.cl:261-483 (the shared-memory path the
+// reference hard-codes): rho and the momentum j = sum e_i f_i.
+template <typename M>
+__device__ __forceinline__ void moments_beta(const M f[19], M &r, M &vx, M &vy, M &vz) {
     r = f[3]; vy = -f[3];
     r += f[2]; vy += f[2];
     r += f[0]; vx = f[0];
@@ -290,34 +315,145 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
     r += f[17]; vz -= f[17];
     r += f[16]; vz += f[16];
     r += f[18];
+}
 
+// Moments in the order of lbm_alpha.cl:61-156.
+template <typename M>
+__device__ __forceinline__ void moments_alpha(const M f[19], M &r, M &vx, M &vy, M &vz) {
+    r = f[0]; vx = f[0];
+    r += f[1]; vx -= f[1];
+    r += f[2]; vy = f[2];
+    r += f[3]; vy -= f[3];
+    r += f[4]; vx += f[4]; vy += f[4];
+    r += f[5]; vx -= f[5]; vy -= f[5];
+    r += f[6]; vx += f[6]; vy -= f[6];
+    r += f[7]; vx -= f[7]; vy += f[7];
+    r += f[8]; vx += f[8]; vz = f[8];
+    r += f[9]; vx -= f[9]; vz -= f[9];
+    r += f[10]; vx += f[10]; vz -= f[10];
+    r += f[11]; vx -= f[11]; vz += f[11];
+    r += f[12]; vy += f[12]; vz += f[12];
+    r += f[13]; vy -= f[13]; vz -= f[13];
+    r += f[14]; vy += f[14]; vz -= f[14];
+    r += f[15]; vy -= f[15]; vz += f[15];
+    r += f[16]; vz += f[16];
+    r += f[17]; vz -= f[17];
+    r += f[18];
+}
+
+// The beta kernel's flag switch (lbm_beta.cl:495-656) on moments already
+// taken: fluid collision (rho becomes dd_param, lbm_beta.cl:493), obstacle
+// bounce-back of the nine opposite pairs, lid equilibrium.  Other flags,
+// the ghost layer included, stream unchanged.
+template <typename M, bool LES>
+__device__ __forceinline__ void beta_case(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    using R = typename Scalar<M>::T;
     if (fl == kFluid) {
-        const R v2 = (vx * vx + vy * vy) + vz * vz;
-        const R dp = r - K<R>::k15 * v2;
-        collide<R, LES>(f, r, vx, vy, vz, dp, d);
-        r = dp;  // dd_param aliases rho (lbm_beta.cl:493)
+        const M v2 = (vx * vx + vy * vy) + vz * vz;
+        const M dp = r - Bc<M>::of(K<R>::k15) * v2;
+        collide<M, LES>(f, r, vx, vy, vz, dp, d);
+        r = dp;
     } else if (fl == kObstacle) {
-        vx = 0; vy = 0; vz = 0;
+        vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
 #pragma unroll
-        for (int k = 0; k < 9; k++) {  // bounce back, lbm_beta.cl:570-578
-            const R t = f[2 * k + 1];
+        for (int k = 0; k < 9; k++) {
+            const M t = f[2 * k + 1];
             f[2 * k + 1] = f[2 * k];
             f[2 * k] = t;
         }
     } else if (fl == kLid) {
-        vx = par<R>(d, P_LID); vy = 0; vz = 0;
-        r = (R)1.0f;
-        const R v2 = (vx * vx + vy * vy) + vz * vz;
-        r = r - K<R>::k15 * v2;
-        equilibria<R>(vx, vy, vz, r, f);
+        vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        r = Bc<M>::of((R)1.0f);
+        const M v2 = (vx * vx + vy * vy) + vz * vz;
+        r = r - Bc<M>::of(K<R>::k15) * v2;
+        equilibria<M>(vx, vy, vz, r, f);
     }
+}
+
+// The alpha kernel's flag switch (lbm_alpha.cl:177-484): returns whether the
+// cell writes its populations (fluid and lid, gravity terms applied).
+template <typename M, bool LES>
+__device__ __forceinline__ bool alpha_case(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    using R = typename Scalar<M>::T;
+    M t[9];
+    if (fl == kFluid) {
+        const M v2 = (vx * vx + vy * vy) + vz * vz;
+        const M dp = r - Bc<M>::of(K<R>::k15) * v2;
+        collide<M, LES>(f, r, vx, vy, vz, dp, d);
+        r = gravity_chain<M>(r, d, t);
+    } else if (fl == kLid) {
+        vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        r = Bc<M>::of((R)1.0f);
+        const M v2 = (vx * vx + vy * vy) + vz * vz;
+        const M dp = r - Bc<M>::of(K<R>::k15) * v2;
+        equilibria<M>(vx, vy, vz, dp, f);
+        r = gravity_chain<M>(r, d, t);
+    } else {
+        if (fl == kObstacle) {  // lbm_alpha.cl:305-343, populations untouched
+            vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        }
+        return false;
+    }
+    if (d.grav) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            f[2 * k + 1] -= t[k];
+            f[2 * k] += t[k];
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ int64_t dir_off(int i, int64_t nx, int64_t slice) {
+    return (int64_t)dir_x(i) + (int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * slice;
+}
+
+// Cell reached from c by the signed offset `off`, wrapped over the whole
+// buffer like the reference's DOMAIN_WRAP (src/cl_programs/wrap.h:112-127).
+__device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) {
+    int64_t i = c + off;
+    if (i < 0) i += n;
+    else if (i >= n) i -= n;
+    return i;
+}
+
+// Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
+// registers) where the one-cell float kernels fit without spilling, fewer
+// for double.
+template <typename S, bool LES, bool BETA>
+__host__ __device__ constexpr int min_blocks() {
+    return sizeof(typename Store<S>::R) == 8 ? 1 : LES ? 4 : (BETA && sizeof(S) == 4) ? 4 : 3;
+}
+
+// ---------------------------------------------------- one cell per thread
+// WRAP: the block holds cells within reach of either end of the buffer;
+// otherwise every neighbour address is the cell's address plus a
+// block-uniform offset.
+template <typename S, bool LES, bool WRAP>
+__device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store_v, int store_rho) {
+    using R = typename Store<S>::R;
+    S *const dd = (S *)d.dd;
+    S *const pc = dd + c;
+    const int64_t ps = d.pstride, nx = d.nx, sl = (int64_t)d.nx * d.ny, n = d.n;
+    const int fl = d.flags[c];
+
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+        const int64_t off = dir_off(i, nx, sl);
+        const S *p = WRAP ? dd + opp(i) * ps + wrap_cell(c, -off, n) : pc + (opp(i) * ps - off);
+        f[i] = Store<S>::ld(p, weight<R>(i));
+    }
+    R r, vx, vy, vz;
+    moments_beta<R>(f, r, vx, vy, vz);
+    beta_case<R, LES>(fl, f, r, vx, vy, vz, d);
 #pragma unroll
     for (int i = 0; i < 19; i++) {
         const int64_t off = dir_off(i, nx, sl);
         S *p = WRAP ? dd + i * ps + wrap_cell(c, off, n) : pc + (i * ps + off);
         Store<S>::st(p, f[i], weight<R>(i));
     }
-    if (fl == kGhost) return;
+    if (fl == kGhost) return;  // lbm_beta.cl:787-788
     if (store_v) {
         R *u = (R *)d.vel + c;
         u[0] = vx; u[n] = vy; u[2 * n] = vz;
@@ -338,79 +474,197 @@ __global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_beta(cons
         beta_cell<S, LES, false>(d, c, a.store_v, a.store_rho);
 }
 
-// ----------------------------------------------------------------- alpha
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ StepArgs a) {
+template <typename S, bool LES>
+__device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int store_v, int store_rho) {
     using R = typename Store<S>::R;
-    const LatDesc &d = lattice_of<PT>(a);
-    const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
-    if (c >= d.n) return;
     const int fl = d.flags[c];
     if (fl == kGhost) return;  // lbm_alpha.cl:31-32
     S *const pc = (S *)d.dd + c;
     const int64_t ps = d.pstride;
-
     R f[19];
 #pragma unroll
     for (int i = 0; i < 19; i++) f[i] = Store<S>::ld(pc + i * ps, weight<R>(i));
-    // moments in the order of lbm_alpha.cl:61-156
     R r, vx, vy, vz;
-    r = f[0]; vx = f[0];
-    r += f[1]; vx -= f[1];
-    r += f[2]; vy = f[2];
-    r += f[3]; vy -= f[3];
-    r += f[4]; vx += f[4]; vy += f[4];
-    r += f[5]; vx -= f[5]; vy -= f[5];
-    r += f[6]; vx += f[6]; vy -= f[6];
-    r += f[7]; vx -= f[7]; vy += f[7];
-    r += f[8]; vx += f[8]; vz = f[8];
-    r += f[9]; vx -= f[9]; vz -= f[9];
-    r += f[10]; vx += f[10]; vz -= f[10];
-    r += f[11]; vx -= f[11]; vz += f[11];
-    r += f[12]; vy += f[12]; vz += f[12];
-    r += f[13]; vy -= f[13]; vz -= f[13];
-    r += f[14]; vy += f[14]; vz -= f[14];
-    r += f[15]; vy -= f[15]; vz += f[15];
-    r += f[16]; vz += f[16];
-    r += f[17]; vz -= f[17];
-    r += f[18];
-
-    bool write = false;
-    R t[9];
-    if (fl == kFluid) {
-        const R v2 = (vx * vx + vy * vy) + vz * vz;
-        const R dp = r - K<R>::k15 * v2;
-        collide<R, LES>(f, r, vx, vy, vz, dp, d);
-        r = gravity_chain<R>(r, d, t);
-        write = true;
-    } else if (fl == kObstacle) {
-        vx = 0; vy = 0; vz = 0;  // lbm_alpha.cl:305-343, populations untouched
-    } else if (fl == kLid) {
-        vx = par<R>(d, P_LID); vy = 0; vz = 0;
-        r = (R)1.0f;
-        const R v2 = (vx * vx + vy * vy) + vz * vz;
-        const R dp = r - K<R>::k15 * v2;
-        equilibria<R>(vx, vy, vz, dp, f);
-        r = gravity_chain<R>(r, d, t);
-        write = true;
-    }
-    if (write) {
-        if (d.grav) {
-#pragma unroll
-            for (int k = 0; k < 9; k++) {
-                f[2 * k + 1] -= t[k];
-                f[2 * k] += t[k];
-            }
-        }
+    moments_alpha<R>(f, r, vx, vy, vz);
+    if (alpha_case<R, LES>(fl, f, r, vx, vy, vz, d)) {
         // each population goes to the opposite slot (lbm_alpha.cl:185-301)
 #pragma unroll
         for (int i = 0; i < 19; i++) Store<S>::st(pc + opp(i) * ps, f[i], weight<R>(i));
     }
-    if (a.store_v) {
+    if (store_v) {
         R *u = (R *)d.vel + c;
         u[0] = vx; u[d.n] = vy; u[2 * d.n] = vz;
     }
-    if (a.store_rho) ((R *)d.rho)[c] = r;
+    if (store_rho) ((R *)d.rho)[c] = r;
+}
+
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ StepArgs a) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
+    if (c >= d.n) return;
+    alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
+}
+
+// ---------------------------------------------------- two cells per thread
+// Thread t of a block owns cells c, c+1 (c even, same x row because nx is
+// even).  Populations along y/z are one aligned 64-bit access per pair.
+// Populations that move along x are one cell off the pair alignment: the
+// missing element comes from the neighbouring lane by a shuffle, and lanes
+// 0 / 31 complete the warp's edge with one scalar access.
+constexpr int kPairCells = 512;  // cells per block of 256 threads
+constexpr unsigned kFull = 0xffffffffu;
+
+// u and rho of a pair; ghost cells store nothing (lbm_beta.cl:787-788).
+__device__ __forceinline__ void store_pair_moments(const LatDesc &d, int64_t c, int fl0, int fl1, P2 r, P2 vx,
+                                                   P2 vy, P2 vz, int store_v, int store_rho) {
+    if (!(store_v | store_rho)) return;
+    const int64_t n = d.n;
+    float *u = (float *)d.vel + c, *rh = (float *)d.rho + c;
+    if (fl0 != kGhost && fl1 != kGhost) {
+        if (store_v) {
+            *(float2 *)u = make_float2(vx.x, vx.y);
+            *(float2 *)(u + n) = make_float2(vy.x, vy.y);
+            *(float2 *)(u + 2 * n) = make_float2(vz.x, vz.y);
+        }
+        if (store_rho) *(float2 *)rh = make_float2(r.x, r.y);
+        return;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        if ((h ? fl1 : fl0) == kGhost) continue;
+        if (store_v) {
+            u[h] = h ? vx.y : vx.x;
+            u[n + h] = h ? vy.y : vy.x;
+            u[2 * n + h] = h ? vz.y : vz.x;
+        }
+        if (store_rho) rh[h] = h ? r.y : r.x;
+    }
+}
+
+template <typename S, bool LES>
+__device__ __forceinline__ void beta_pair(const LatDesc &d, int64_t c, int lane, int store_v, int store_rho) {
+    using R = float;
+    S *const dd = (S *)d.dd;
+    const int64_t ps = d.pstride, nx = d.nx, sl = (int64_t)d.nx * d.ny;
+    const uint16_t fl2 = *(const uint16_t *)(d.flags + c);
+    const int fl0 = fl2 & 0xff, fl1 = fl2 >> 8;
+
+    P2 f[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+        const int ex = dir_x(i);
+        const R w = weight<R>(i);
+        // aligned pair (c, c+1) of the source row: c - e_i without its x part
+        const S *p = dd + opp(i) * ps + c - ((int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * sl);
+        const P2 q = Store<S>::ld2(p, w);
+        if (ex == 0) {
+            f[i] = q;
+        } else if (ex > 0) {  // sources (c-1, c)
+            float lo = __shfl_up_sync(kFull, q.y, 1);
+            if (lane == 0) lo = Store<S>::ld(p - 1, w);
+            f[i] = P2{lo, q.x};
+        } else {  // sources (c+1, c+2)
+            float hi = __shfl_down_sync(kFull, q.x, 1);
+            if (lane == 31) hi = Store<S>::ld(p + 2, w);
+            f[i] = P2{q.y, hi};
+        }
+    }
+    P2 r, vx, vy, vz;
+    moments_beta<P2>(f, r, vx, vy, vz);
+    if (fl0 == kFluid && fl1 == kFluid) {
+        beta_case<P2, LES>(kFluid, f, r, vx, vy, vz, d);
+    } else {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            R g[19], rr = h ? r.y : r.x, ux = h ? vx.y : vx.x, uy = h ? vy.y : vy.x, uz = h ? vz.y : vz.x;
+#pragma unroll
+            for (int i = 0; i < 19; i++) g[i] = h ? f[i].y : f[i].x;
+            beta_case<R, LES>(h ? fl1 : fl0, g, rr, ux, uy, uz, d);
+#pragma unroll
+            for (int i = 0; i < 19; i++) (h ? f[i].y : f[i].x) = g[i];
+            (h ? r.y : r.x) = rr; (h ? vx.y : vx.x) = ux; (h ? vy.y : vy.x) = uy; (h ? vz.y : vz.x) = uz;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+        const int ex = dir_x(i);
+        const R w = weight<R>(i);
+        S *p = dd + i * ps + c + ((int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * sl);
+        if (ex == 0) {
+            Store<S>::st2(p, f[i], w);
+        } else if (ex > 0) {  // destinations (c+1, c+2)
+            const float lo = __shfl_up_sync(kFull, f[i].y, 1);
+            if (lane != 0) Store<S>::st2(p, P2{lo, f[i].x}, w);
+            else Store<S>::st(p + 1, f[i].x, w);
+            if (lane == 31) Store<S>::st(p + 2, f[i].y, w);
+        } else {  // destinations (c-1, c)
+            const float hi = __shfl_down_sync(kFull, f[i].x, 1);
+            if (lane != 31) Store<S>::st2(p, P2{f[i].y, hi}, w);
+            else Store<S>::st(p, f[i].y, w);
+            if (lane == 0) Store<S>::st(p - 1, f[i].x, w);
+        }
+    }
+    store_pair_moments(d, c, fl0, fl1, r, vx, vy, vz, store_v, store_rho);
+}
+
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, 2) k_beta2(const __grid_constant__ StepArgs a) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * kPairCells;
+    const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny + 2;
+    if (c0 < reach || c0 + kPairCells + reach >= d.n) {
+        // near either end of the buffer: one cell at a time with the wrap
+        for (int h = 0; h < 2; h++) {
+            const int64_t c = c0 + 2 * threadIdx.x + h;
+            if (c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+        }
+        return;
+    }
+    beta_pair<S, LES>(d, c0 + 2 * threadIdx.x, threadIdx.x & 31, a.store_v, a.store_rho);
+}
+
+template <typename S, bool LES>
+__device__ __forceinline__ void alpha_pair(const LatDesc &d, int64_t c, int store_v, int store_rho) {
+    using R = float;
+    S *const pc = (S *)d.dd + c;
+    const int64_t ps = d.pstride;
+    const uint16_t fl2 = *(const uint16_t *)(d.flags + c);
+    const int fl0 = fl2 & 0xff, fl1 = fl2 >> 8;
+    if (fl0 == kGhost && fl1 == kGhost) return;  // lbm_alpha.cl:31-32
+    P2 f[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) f[i] = Store<S>::ld2(pc + i * ps, weight<R>(i));
+    P2 r, vx, vy, vz;
+    moments_alpha<P2>(f, r, vx, vy, vz);
+    if (fl0 == kFluid && fl1 == kFluid) {
+        alpha_case<P2, LES>(kFluid, f, r, vx, vy, vz, d);
+#pragma unroll
+        for (int i = 0; i < 19; i++) Store<S>::st2(pc + opp(i) * ps, f[i], weight<R>(i));
+    } else {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int fl = h ? fl1 : fl0;
+            if (fl == kGhost) continue;
+            R g[19], rr = h ? r.y : r.x, ux = h ? vx.y : vx.x, uy = h ? vy.y : vy.x, uz = h ? vz.y : vz.x;
+#pragma unroll
+            for (int i = 0; i < 19; i++) g[i] = h ? f[i].y : f[i].x;
+            if (alpha_case<R, LES>(fl, g, rr, ux, uy, uz, d)) {
+#pragma unroll
+                for (int i = 0; i < 19; i++) Store<S>::st(pc + opp(i) * ps + h, g[i], weight<R>(i));
+            }
+            (h ? r.y : r.x) = rr; (h ? vx.y : vx.x) = ux; (h ? vy.y : vy.x) = uy; (h ? vz.y : vz.x) = uz;
+        }
+    }
+    store_pair_moments(d, c, fl0, fl1, r, vx, vy, vz, store_v, store_rho);
+}
+
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ StepArgs a) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c = (int64_t)(blockIdx.x - d.first_block) * kPairCells + 2 * threadIdx.x;
+    if (c + 1 < d.n) alpha_pair<S, LES>(d, c, a.store_v, a.store_rho);
+    else if (c < d.n) alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
 }
 
 }  // namespace lbm
