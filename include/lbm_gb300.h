@@ -140,6 +140,20 @@ int lbm_cu_halo(lbm_lattice *src, const int src_origin[3], lbm_lattice *dst, con
  * No reference counterpart. */
 int lbm_cu_reduce_conserved(lbm_lattice *lat, int layout, double out[5], void *stream);
 
+/* The same sums, for callers that must not allocate device memory (no
+ * counterpart in the reference).  lbm_cu_reduce_conserved may grow the
+ * lattice's staging buffer with cudaMalloc; a serving loop whose HBM is all
+ * handed out under a budget, or a monitor that must not trigger the implicit
+ * synchronisation of cudaMalloc/cudaFree, cannot afford that.  This variant
+ * keeps its partial sums in a fixed device array inside the library
+ * (1.3 MB, present on every GPU that loads the library until the process
+ * exits) and calls no allocator.  Limit: lattices of at most 134,217,728
+ * cells (512^3); larger ones are rejected with an error.  The first call on
+ * a device looks up the array's device address, so make that first call
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race and must be ordered by the caller. */
+int lbm_cu_reduce_conserved_noalloc(lbm_lattice *lat, int layout, double out[5], void *stream);
+
 /* ----------------------------------------------------------------- domain */
 
 /* A decomposed domain held on one GPU: the even split and CComm geometry of

@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
         "lbm_cu_write": ([vp, ci, ip, ip, vp, ip, vp], ci),
         "lbm_cu_halo": ([vp, ip, vp, ip, ip, ip, vp], ci),
         "lbm_cu_reduce_conserved": ([vp, ci, C.POINTER(cd), vp], ci),
+        "lbm_cu_reduce_conserved_noalloc": ([vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_domain_create": ([ip, ip, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_domain_destroy": ([vp], ci),
         "lbm_cu_domain_set_params": ([vp, C.POINTER(Params)], ci),
@@ -184,6 +185,13 @@ class Lattice:
     def reduce_conserved(self, layout: int, stream=None):
         out = (C.c_double * 5)()
         check(lib().lbm_cu_reduce_conserved(self.h, layout, out, stream))
+        return np.array(out[:], dtype=np.float64)
+
+    def reduce_conserved_noalloc(self, layout: int, stream=None):
+        """The same sums without any device allocation (fixed in-library
+        scratch, lattices up to 512^3 cells); see include/lbm_gb300.h."""
+        out = (C.c_double * 5)()
+        check(lib().lbm_cu_reduce_conserved_noalloc(self.h, layout, out, stream))
         return np.array(out[:], dtype=np.float64)
 
 

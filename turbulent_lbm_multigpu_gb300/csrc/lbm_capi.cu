@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -737,6 +738,69 @@ int lbm_cu_reduce_conserved(lbm_lattice *l, int layout, double out[5], void *str
 }
 
 }  // extern "C"
+
+// ------------------------------------------ reduction without allocation
+// Some callers must not allocate device memory: a serving loop that has
+// handed every free byte of HBM to resident fields under a budget, a monitor
+// thread that checks conservation while other streams run and cannot take
+// the device-wide synchronisation cudaMalloc/cudaFree may imply, or a host
+// framework whose own allocator owns the device.  For them the partial sums
+// of the conservation reduction live in this fixed array instead of the
+// lattice's staging buffer: one partial (sum and compensation of 5
+// quantities) per block of 256 threads x 32 cells, at most kStaticPartials
+// blocks, so lattices of up to kStaticPartials * kStaticCellsPerBlock cells.
+// The array exists once per GPU that loads this library and stays allocated
+// until the process exits.  Every call reuses it: each call writes every
+// partial it later reads, so nothing has to be cleared, but two calls whose
+// work overlaps on the GPU (different streams, no ordering) race on it.
+constexpr int kStaticPartials = 16384;
+constexpr int64_t kStaticCellsPerBlock = (int64_t)kBlock * 32;
+static __device__ __align__(256) double g_reduce_scratch[kStaticPartials * 10 + 8];
+
+namespace {
+// Device address of g_reduce_scratch, looked up once per device with that
+// device current (the host-side symbol is not a device address).
+int static_scratch(double **out) {
+    static std::mutex mu;
+    static double *addr[128] = {};
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return fail("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        CU(cudaGetSymbolAddress(&p, g_reduce_scratch));
+        addr[dev] = (double *)p;
+    }
+    *out = addr[dev];
+    return 0;
+}
+}  // namespace
+
+extern "C" int lbm_cu_reduce_conserved_noalloc(lbm_lattice *l, int layout, double out[5], void *stream) {
+    if (!l || !out) return fail("NULL argument");
+    const int64_t max_cells = (int64_t)kStaticPartials * kStaticCellsPerBlock;
+    if (l->n > max_cells)
+        return fail("lattice has " + std::to_string(l->n) + " cells; the no-allocation reduction handles at most " +
+                    std::to_string(max_cells));
+    double *partial = nullptr;
+    if (static_scratch(&partial)) return -1;
+    double *res = partial + (size_t)kStaticPartials * 10;
+    const int blocks = (int)std::max<int64_t>(1, (l->n + kStaticCellsPerBlock - 1) / kStaticCellsPerBlock);
+    cudaStream_t st = S(stream);
+    switch (l->storage) {
+        case kF32: k_reduce<float><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kF64: k_reduce<double><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kF16: k_reduce<__half><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kBF16: k_reduce<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+    }
+    CU(cudaGetLastError());
+    k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, res);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return 0;
+}
 
 // ================================================================== domain
 struct CommGeom {
