@@ -199,6 +199,68 @@ int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
 int lbm_cu_domain_subdomains(const lbm_domain *dom, int *count, int sub_size[3]);
 lbm_lattice *lbm_cu_domain_lattice(lbm_domain *dom, int index);
 
+/* ------------------------------------------------------ batches, serving */
+
+/* One lid-driven cavity of an ensemble, in lattice units: walls on all six
+ * faces and the lid plane of CController::setGeometry
+ * (src/CController.hpp:531-546) moving at `lid`; relaxation time tau0,
+ * Smagorinsky constant cs (0 = plain BGK); `steps` time steps; optional
+ * seeded start-up velocity amplitude `amp` (0 = rest).  No reference
+ * counterpart (the reference runs one domain per process). */
+typedef struct lbm_cavity {
+    int nx, ny, nz;
+    int storage;
+    double tau0;
+    double cs;
+    double lid;
+    int64_t steps;
+    uint64_t seed;
+    double amp;
+} lbm_cavity;
+
+typedef struct lbm_batch lbm_batch;
+typedef struct lbm_server lbm_server;
+
+/* `steps` time steps of one lattice whose step counter is `first_step`, one
+ * launch per step (CLbmSolver::simulationStep in a loop). */
+int lbm_cu_run(lbm_lattice *lat, int64_t first_step, int64_t steps, void *stream);
+
+/* An ensemble of cavities of different sizes, parameters, storage types and
+ * step counts, all resident, advanced together: one launch per storage type
+ * and step covers every unfinished cavity, pairs of steps replay a captured
+ * CUDA graph, every cavity stops at its own step count.  Each cavity's
+ * fields are the same as when it runs alone (lbm_cu_batch_lattice gives
+ * its lattice for readback; velocity is written on its last step when
+ * store_velocity is set). */
+int lbm_cu_batch_create(const lbm_cavity *cavities, int count, int store_velocity, lbm_batch **out);
+int lbm_cu_batch_destroy(lbm_batch *b);
+int lbm_cu_batch_reset(lbm_batch *b, void *stream);
+int lbm_cu_batch_set_kernel_shape(lbm_batch *b, int cells_per_thread);
+/* Autotuner: times `trial_steps` steps of the whole ensemble for each kernel
+ * shape (one or two cells per thread), keeps the fastest, and resets. */
+int lbm_cu_batch_tune(lbm_batch *b, int trial_steps, int *cells_per_thread, double *ms_per_step, void *stream);
+/* Run until every cavity has taken its steps, or at most max_steps steps
+ * (max_steps < 0: no limit). */
+int lbm_cu_batch_run(lbm_batch *b, int64_t max_steps, int use_graph, void *stream);
+int lbm_cu_batch_status(const lbm_batch *b, int64_t *min_done, int *active);
+lbm_lattice *lbm_cu_batch_lattice(lbm_batch *b, int index);
+
+/* Continuous-batching solve server.  Submitted solves queue; each tick
+ * admits queued solves in arrival order while their device memory fits the
+ * HBM budget (and fewer than max_active run), advances every running solve
+ * by up to max_steps steps in shared launches (stopping when the first one
+ * completes), and retires completed solves, whose fields stay resident
+ * until released.  A solve's result does not depend on what else runs. */
+int lbm_cu_server_create(double hbm_budget_bytes, int max_active, int store_velocity, lbm_server **out);
+int lbm_cu_server_destroy(lbm_server *s);
+int lbm_cu_server_set_kernel_shape(lbm_server *s, int cells_per_thread);
+int lbm_cu_server_submit(lbm_server *s, const lbm_cavity *c, int64_t *id);
+int lbm_cu_server_tick(lbm_server *s, int64_t max_steps, int use_graph, int *admitted, void *stream);
+int lbm_cu_server_poll(lbm_server *s, int64_t *ids, int capacity, int *count);
+lbm_lattice *lbm_cu_server_lattice(lbm_server *s, int64_t id);
+int lbm_cu_server_release(lbm_server *s, int64_t id);
+int lbm_cu_server_status(const lbm_server *s, int *queued, int *active, double *hbm_used, int64_t *cell_updates);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,21 @@ class LbmError(RuntimeError):
     pass
 
 
+class Cavity(C.Structure):
+    """lbm_cavity: one lid-driven cavity of an ensemble (lattice units)."""
+
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("storage", C.c_int),
+                ("tau0", C.c_double), ("cs", C.c_double), ("lid", C.c_double), ("steps", C.c_int64),
+                ("seed", C.c_uint64), ("amp", C.c_double)]
+
+    @staticmethod
+    def make(dims, storage=0, tau0=0.6, cs=0.0, lid=0.05, steps=100, seed=0, amp=0.0):
+        c = Cavity()
+        c.nx, c.ny, c.nz = (int(x) for x in dims)
+        c.storage, c.tau0, c.cs, c.lid, c.steps, c.seed, c.amp = storage, tau0, cs, lid, int(steps), seed, amp
+        return c
+
+
 class Params(C.Structure):
     """lbm_params: kernel arguments in double (rounded to the arithmetic type by the library)."""
 
@@ -88,6 +103,24 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
         "lbm_cu_domain_lattice": ([vp, ci], vp),
+        "lbm_cu_run": ([vp, i64, i64, vp], ci),
+        "lbm_cu_batch_create": ([C.POINTER(Cavity), ci, ci, C.POINTER(vp)], ci),
+        "lbm_cu_batch_destroy": ([vp], ci),
+        "lbm_cu_batch_reset": ([vp, vp], ci),
+        "lbm_cu_batch_set_kernel_shape": ([vp, ci], ci),
+        "lbm_cu_batch_tune": ([vp, ci, ip, C.POINTER(cd), vp], ci),
+        "lbm_cu_batch_run": ([vp, i64, ci, vp], ci),
+        "lbm_cu_batch_status": ([vp, C.POINTER(i64), ip], ci),
+        "lbm_cu_batch_lattice": ([vp, ci], vp),
+        "lbm_cu_server_create": ([cd, ci, ci, C.POINTER(vp)], ci),
+        "lbm_cu_server_destroy": ([vp], ci),
+        "lbm_cu_server_set_kernel_shape": ([vp, ci], ci),
+        "lbm_cu_server_submit": ([vp, C.POINTER(Cavity), C.POINTER(i64)], ci),
+        "lbm_cu_server_tick": ([vp, i64, ci, ip, vp], ci),
+        "lbm_cu_server_poll": ([vp, C.POINTER(i64), ci, ip], ci),
+        "lbm_cu_server_lattice": ([vp, i64], vp),
+        "lbm_cu_server_release": ([vp, i64], ci),
+        "lbm_cu_server_status": ([vp, ip, ip, C.POINTER(cd), C.POINTER(i64)], ci),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -182,6 +215,10 @@ class Lattice:
         check(lib().lbm_cu_write(self.h, field, ivec(origin), ivec(size), src.ctypes.data_as(C.c_void_p),
                                  ivec(norm), stream))
 
+    def run(self, first_step: int, steps: int, stream=None):
+        """`steps` steps, one launch each, starting at step counter `first_step`."""
+        check(lib().lbm_cu_run(self.h, first_step, steps, stream))
+
     def reduce_conserved(self, layout: int, stream=None):
         out = (C.c_double * 5)()
         check(lib().lbm_cu_reduce_conserved(self.h, layout, out, stream))
@@ -266,3 +303,104 @@ class Domain:
         ms, n = C.c_double(), C.c_int64()
         check(lib().lbm_cu_domain_kernel_time(self.h, C.byref(ms), C.byref(n), int(reset)))
         return ms.value, n.value
+
+
+class Batch:
+    """An ensemble of cavities advanced together (lbm_cu_batch_*)."""
+
+    def __init__(self, cavities, store_velocity=True):
+        arr = (Cavity * len(cavities))(*cavities)
+        h = C.c_void_p()
+        check(lib().lbm_cu_batch_create(arr, len(cavities), int(store_velocity), C.byref(h)))
+        self.h = h
+        self.cavities = list(cavities)
+        self.lattices = [Lattice(c.nx, c.ny, c.nz, c.storage, store_velocity, False,
+                                 handle=lib().lbm_cu_batch_lattice(self.h, i), owner=self)
+                         for i, c in enumerate(self.cavities)]
+
+    def close(self):
+        if self.h:
+            lib().lbm_cu_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self, stream=None):
+        check(lib().lbm_cu_batch_reset(self.h, stream))
+
+    def set_kernel_shape(self, cells_per_thread):
+        check(lib().lbm_cu_batch_set_kernel_shape(self.h, cells_per_thread))
+
+    def tune(self, trial_steps=20, stream=None):
+        shape, ms = C.c_int(), C.c_double()
+        check(lib().lbm_cu_batch_tune(self.h, trial_steps, C.byref(shape), C.byref(ms), stream))
+        return shape.value, ms.value
+
+    def run(self, max_steps=-1, use_graph=True, stream=None):
+        check(lib().lbm_cu_batch_run(self.h, max_steps, int(use_graph), stream))
+
+    def status(self):
+        done, active = C.c_int64(), C.c_int()
+        check(lib().lbm_cu_batch_status(self.h, C.byref(done), C.byref(active)))
+        return done.value, active.value
+
+
+class Server:
+    """Continuous-batching solve server (lbm_cu_server_*)."""
+
+    def __init__(self, hbm_budget_bytes, max_active=0, store_velocity=True):
+        h = C.c_void_p()
+        check(lib().lbm_cu_server_create(float(hbm_budget_bytes), max_active, int(store_velocity), C.byref(h)))
+        self.h = h
+        self.store_velocity = store_velocity
+        self.specs = {}
+
+    def close(self):
+        if self.h:
+            lib().lbm_cu_server_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_kernel_shape(self, cells_per_thread):
+        check(lib().lbm_cu_server_set_kernel_shape(self.h, cells_per_thread))
+
+    def submit(self, cavity: Cavity) -> int:
+        i = C.c_int64()
+        check(lib().lbm_cu_server_submit(self.h, C.byref(cavity), C.byref(i)))
+        self.specs[i.value] = cavity
+        return i.value
+
+    def tick(self, max_steps=-1, use_graph=True, stream=None) -> int:
+        adm = C.c_int()
+        check(lib().lbm_cu_server_tick(self.h, max_steps, int(use_graph), C.byref(adm), stream))
+        return adm.value
+
+    def poll(self, capacity=4096):
+        ids = (C.c_int64 * capacity)()
+        n = C.c_int()
+        check(lib().lbm_cu_server_poll(self.h, ids, capacity, C.byref(n)))
+        return list(ids[:n.value])
+
+    def lattice(self, sid) -> Lattice:
+        c = self.specs[sid]
+        h = lib().lbm_cu_server_lattice(self.h, sid)
+        if not h:
+            raise LbmError(lib().lbm_cu_last_error().decode())
+        return Lattice(c.nx, c.ny, c.nz, c.storage, self.store_velocity, False, handle=h, owner=self)
+
+    def release(self, sid):
+        check(lib().lbm_cu_server_release(self.h, sid))
+
+    def status(self):
+        q, a, used, cu = C.c_int(), C.c_int(), C.c_double(), C.c_int64()
+        check(lib().lbm_cu_server_status(self.h, C.byref(q), C.byref(a), C.byref(used), C.byref(cu)))
+        return {"queued": q.value, "active": a.value, "hbm_used": used.value, "cell_updates": cu.value}

@@ -14,55 +14,21 @@
 #include <string>
 #include <vector>
 
-#include "lbm_gb300.h"
-#include "lbm_kernels.cuh"
+#include "lbm_internal.h"
 
 using namespace lbm;
+using namespace lbm_rt;
 
-namespace {
+namespace lbm_rt {
 thread_local std::string g_err;
 
 int fail(const std::string &m) {
     g_err = m;
     return -1;
 }
+}  // namespace lbm_rt
 
-#define CU(call)                                                                          \
-    do {                                                                                  \
-        cudaError_t e_ = (call);                                                          \
-        if (e_ != cudaSuccess) return fail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
-
-constexpr int kBlock = 256;
-
-size_t storage_bytes(int st) { return st == kF64 ? 8 : st == kF32 ? 4 : 2; }
-size_t real_bytes(int st) { return st == kF64 ? 8 : 4; }
-
-int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
-
-bool valid_box(const lbm_lattice *l, const int o[3], const int s[3]);
-}  // namespace
-
-struct lbm_lattice {
-    int nx, ny, nz;
-    int64_t n, pstride;
-    int storage;
-    int store_v, store_rho;
-    void *dd = nullptr;
-    uint8_t *flags = nullptr;
-    void *vel = nullptr;
-    void *rho = nullptr;
-    LatDesc h{};
-    LatDesc *d_desc = nullptr;
-    bool dirty = true;
-    void *stage = nullptr;  // staging for host copies and reduction partials
-    size_t stage_bytes = 0;
-    bool allow_pair = false;  // two-cell kernels where the shape allows (tuning option)
-};
-
-namespace {
+namespace lbm_rt {
 bool valid_box(const lbm_lattice *l, const int o[3], const int s[3]) {
     const int d[3] = {l->nx, l->ny, l->nz};
     for (int a = 0; a < 3; a++)
@@ -118,8 +84,6 @@ void set_params_desc(LatDesc &h, int storage, const lbm_params &p) {
     }
     h.grav = grav;
 }
-
-bool uses_les(const LatDesc &h) { return h.pd[P_LES] != 0.0; }
 
 // ---------------------------------------------------------------- kernels
 template <typename S>
@@ -407,8 +371,6 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab) {
     return true;
 }
 
-int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
-
 // One step over `ntab` lattices.  `htab` holds the host copy of the
 // descriptors with first_block/nblocks for the launch shape; the launch uses
 // it as kernel parameters when it fits, else the device copy `dtab`.
@@ -438,8 +400,6 @@ int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *hta
     }
     return fail("unknown storage type");
 }
-
-int grid_for(int64_t work) { return (int)((work + kBlock - 1) / kBlock); }
 
 Box make_box(const lbm_lattice *l, const int o[3], const int s[3]) {
     Box b;
@@ -485,7 +445,7 @@ int launch_halo_batch(int storage, const HaloDesc *d_hd, int nd, int64_t max_cel
     CU(cudaGetLastError());
     return 0;
 }
-}  // namespace
+}  // namespace lbm_rt
 
 // =================================================================== C ABI
 extern "C" {

@@ -1,0 +1,64 @@
+// lbm_internal.h -- host runtime shared by the translation units of
+// liblbm_gb300.so (not part of the public C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "lbm_gb300.h"
+#include "lbm_kernels.cuh"
+
+namespace lbm_rt {
+using namespace lbm;
+
+// Records the message returned by lbm_cu_last_error() on this thread; -1.
+int fail(const std::string &m);
+
+#define CU(call)                                                                                \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess) return ::lbm_rt::fail(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+inline cudaStream_t S(void *s) { return (cudaStream_t)s; }
+
+constexpr int kBlock = 256;
+
+inline size_t storage_bytes(int st) { return st == kF64 ? 8 : st == kF32 ? 4 : 2; }
+inline size_t real_bytes(int st) { return st == kF64 ? 8 : 4; }
+inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+inline int grid_for(int64_t work) { return (int)((work + kBlock - 1) / kBlock); }
+
+// Kernel arguments of a lattice, rounded to its arithmetic type.
+void set_params_desc(LatDesc &h, int storage, const lbm_params &p);
+inline bool uses_les(const LatDesc &h) { return h.pd[P_LES] != 0.0; }
+
+// The two-cell kernels apply when every lattice has an even x extent and a
+// float arithmetic type.
+bool pair_shape(int storage, const LatDesc *tab, int ntab);
+inline int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
+
+// One step over `ntab` lattices of one storage type; `htab` holds the
+// descriptors with first_block/nblocks for the launch shape, used as
+// kernel parameters when they fit, else the device copy `dtab`.
+int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab,
+                int blocks, int sv, int sr, cudaStream_t st);
+}  // namespace lbm_rt
+
+struct lbm_lattice {
+    int nx, ny, nz;
+    int64_t n, pstride;
+    int storage;
+    int store_v, store_rho;
+    void *dd = nullptr;
+    uint8_t *flags = nullptr;
+    void *vel = nullptr;
+    void *rho = nullptr;
+    lbm::LatDesc h{};
+    lbm::LatDesc *d_desc = nullptr;
+    bool dirty = true;
+    void *stage = nullptr;  // staging for host copies and reduction partials
+    size_t stage_bytes = 0;
+    bool allow_pair = false;  // two-cell kernels where the shape allows (tuning option)
+};

@@ -156,6 +156,7 @@ struct LatDesc {
     int32_t first_block;  // first block of this lattice in a batched launch
     int32_t nblocks;      // blocks of the launched kernel shape
     int32_t grav;         // gravity chain non-zero (alpha kernel)
+    int32_t parity;       // step counter parity at the start of a batch tick
     double pd[16];        // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
     float pf[16];
 };
@@ -665,6 +666,49 @@ __global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ StepA
     const int64_t c = (int64_t)(blockIdx.x - d.first_block) * kPairCells + 2 * threadIdx.x;
     if (c + 1 < d.n) alpha_pair<S, LES>(d, c, a.store_v, a.store_rho);
     else if (c < d.n) alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
+}
+
+// ------------------------------------------------ batches of lattices
+// Every lattice of a batch keeps its own step counter: step j of a tick is
+// a beta step for a lattice whose counter was even at the tick start and j
+// even (and so on), chosen per block.  Used for ensembles of cavities and
+// for the serving loop, where solves start at different times.
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_step(const __grid_constant__ StepArgs a, int j) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
+    const int64_t c = c0 + threadIdx.x;
+    if (c >= d.n) return;
+    if ((d.parity + j) & 1) {
+        alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
+        return;
+    }
+    const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny;
+    if (c0 < reach || c0 + (int64_t)blockDim.x - 1 + reach >= d.n)
+        beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+    else
+        beta_cell<S, LES, false>(d, c, a.store_v, a.store_rho);
+}
+
+template <typename S, bool LES, bool PT>
+__global__ void __launch_bounds__(256, 2) k_step2(const __grid_constant__ StepArgs a, int j) {
+    const LatDesc &d = lattice_of<PT>(a);
+    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * kPairCells;
+    if ((d.parity + j) & 1) {
+        const int64_t c = c0 + 2 * threadIdx.x;
+        if (c + 1 < d.n) alpha_pair<S, LES>(d, c, a.store_v, a.store_rho);
+        else if (c < d.n) alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
+        return;
+    }
+    const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny + 2;
+    if (c0 < reach || c0 + kPairCells + reach >= d.n) {
+        for (int h = 0; h < 2; h++) {
+            const int64_t c = c0 + 2 * threadIdx.x + h;
+            if (c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+        }
+        return;
+    }
+    beta_pair<S, LES>(d, c0 + 2 * threadIdx.x, threadIdx.x & 31, a.store_v, a.store_rho);
 }
 
 }  // namespace lbm
