@@ -330,6 +330,20 @@ def run_gpu(args):
                             "frac_of_measured_hbm": round(xa / peak, 4), "steps": n,
                             "alg_bytes_per_cell": BYTES_PER_CELL[st]}
 
+    if not args.no_extra and tuple(args.size) == SIZE:
+        from turbulent_lbm_multigpu_gb300 import experiments as ex
+
+        b = ex.batch(count=512, scale=10.0, check=2)
+        extra["batch 512 cavities (steps/10)"] = {k: (round(v, 3) if isinstance(v, float) else v)
+                                                 for k, v in b.items() if k != "config"}
+        extra["batch 512 cavities (steps/10)"]["cell_updates"] = b["config"]["cell_updates"]
+        sv = ex.serve(requests=24, scale=20.0, rates=(100, 400))
+        extra["serving 24 requests (steps/20)"] = {
+            "sequential_plain_f32_solves_per_s": round(sv["sequential_plain_f32"]["solves_per_s"], 3),
+            "served": [{k: round(v, 4) for k, v in r.items()} for r in sv["served"]],
+            "speedup_solves_per_s": [round(x, 3) for x in sv["speedup_solves_per_s"]],
+            "f16_share": sv["config"]["f16_share"]}
+
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,

@@ -140,6 +140,14 @@ int lbm_cu_halo(lbm_lattice *src, const int src_origin[3], lbm_lattice *dst, con
  * No reference counterpart. */
 int lbm_cu_reduce_conserved(lbm_lattice *lat, int layout, double out[5], void *stream);
 
+/* Velocity error of lattice a against lattice b (same size) over the fluid
+ * cells of a, in FP64: out = {max |ua - ub|, sum |ua - ub|^2, sum |ub|^2,
+ * max |ub|, number of cells}, u = sum_i e_i f_i of the stored populations
+ * in each lattice's slot layout.  For precision studies against an FP64
+ * run; no reference counterpart. */
+int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int layout_b, double out[5],
+                            void *stream);
+
 /* The same sums, for callers that must not allocate device memory (no
  * counterpart in the reference).  lbm_cu_reduce_conserved may grow the
  * lattice's staging buffer with cudaMalloc; a serving loop whose HBM is all

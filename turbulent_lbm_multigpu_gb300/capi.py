@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "lbm_cu_halo": ([vp, ip, vp, ip, ip, ip, vp], ci),
         "lbm_cu_reduce_conserved": ([vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_reduce_conserved_noalloc": ([vp, ci, C.POINTER(cd), vp], ci),
+        "lbm_cu_compare_velocity": ([vp, ci, vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_domain_create": ([ip, ip, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_domain_destroy": ([vp], ci),
         "lbm_cu_domain_set_params": ([vp, C.POINTER(Params)], ci),
@@ -230,6 +231,16 @@ class Lattice:
         out = (C.c_double * 5)()
         check(lib().lbm_cu_reduce_conserved_noalloc(self.h, layout, out, stream))
         return np.array(out[:], dtype=np.float64)
+
+
+def compare_velocity(a: Lattice, layout_a: int, b: Lattice, layout_b: int, stream=None):
+    """{max_abs, rms, rel_rms, rel_max, cells} of a's velocity against b's over a's fluid cells."""
+    out = (C.c_double * 5)()
+    check(lib().lbm_cu_compare_velocity(a.h, layout_a, b.h, layout_b, out, stream))
+    mx, se, sr, mr, n = out[:]
+    n = max(n, 1.0)
+    return {"max_abs": mx, "rms": math.sqrt(se / n), "rel_rms": math.sqrt(se / sr) if sr > 0 else 0.0,
+            "rel_max": mx / mr if mr > 0 else 0.0, "ref_rms": math.sqrt(sr / n), "ref_max": mr, "cells": int(n)}
 
 
 def halo(src: Lattice, src_origin, dst: Lattice, dst_origin, size, norm=None, stream=None):

@@ -121,6 +121,7 @@ struct Ensemble {
         std::vector<int> members;
         std::vector<LatDesc> htab;
         LatDesc *dtab = nullptr;
+        int32_t *dmap = nullptr;  // lattice index of every block
         size_t cap = 0;
         int blocks = 0;
     };
@@ -135,8 +136,10 @@ struct Ensemble {
     ~Ensemble() {
         drop_graph();
         if (cap) cudaStreamDestroy(cap);
-        for (auto &g : groups)
+        for (auto &g : groups) {
             if (g.dtab) cudaFree(g.dtab);
+            if (g.dmap) cudaFree(g.dmap);
+        }
         for (auto &s : slots)
             if (s.lat) lbm_cu_destroy(s.lat);
     }
@@ -147,8 +150,10 @@ struct Ensemble {
 
     // Descriptor tables of the active cavities, one group per (storage, shape).
     int build_groups() {
-        for (auto &g : groups)
+        for (auto &g : groups) {
             if (g.dtab) cudaFree(g.dtab);
+            if (g.dmap) cudaFree(g.dmap);
+        }
         groups.clear();
         for (size_t i = 0; i < slots.size(); i++) {
             const Slot &s = slots[i];
@@ -168,6 +173,14 @@ struct Ensemble {
         for (auto &g : groups) {
             g.cap = g.members.size();
             CU(cudaMalloc((void **)&g.dtab, g.cap * sizeof(LatDesc)));
+            const int per = cells_per_block(g.pair);
+            std::vector<int32_t> map;
+            for (size_t k = 0; k < g.members.size(); k++) {
+                const int64_t n = slots[g.members[k]].lat->n;
+                map.insert(map.end(), (size_t)((n + per - 1) / per), (int32_t)k);
+            }
+            CU(cudaMalloc((void **)&g.dmap, map.size() * sizeof(int32_t)));
+            CU(cudaMemcpy(g.dmap, map.data(), map.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
         }
         dirty = false;
         drop_graph();
@@ -202,6 +215,7 @@ struct Ensemble {
             memset(&a, 0, sizeof(a));
             a.ntab = (int)g.htab.size();
             a.dtab = g.dtab;
+            a.block_lattice = g.dmap;
             a.store_v = store ? store_v : 0;
             a.store_rho = 0;
             // the tick kernels always read the device table, so a captured

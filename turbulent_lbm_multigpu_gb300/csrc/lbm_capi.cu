@@ -326,6 +326,63 @@ __global__ void __launch_bounds__(kBlock) k_reduce(LatDesc d, int layout, double
         }
 }
 
+// Velocity difference of two lattices of the same size over the fluid cells
+// of `a`: max |ua - ub|, sum |ua - ub|^2, sum |ub|^2, max |ub|, cell count,
+// with u the momentum of the stored populations in the given slot layouts.
+template <typename SA, typename SB>
+__global__ void __launch_bounds__(kBlock) k_compare(LatDesc a, int la, LatDesc b, int lb, double *partial) {
+    using RA = typename Store<SA>::R;
+    using RB = typename Store<SB>::R;
+    __shared__ double sh[5][kBlock];
+    double mx = 0, se = 0, sr = 0, mr = 0, cnt = 0;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (a.flags[c] != kFluid) continue;
+        double ua[3] = {0, 0, 0}, ub[3] = {0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < 19; i++) {
+            const int sa = la ? opp(i) : i, sb = lb ? opp(i) : i;
+            const double fa = (double)Store<SA>::ld((const SA *)a.dd + sa * a.pstride + c, weight<RA>(sa));
+            const double fb = (double)Store<SB>::ld((const SB *)b.dd + sb * b.pstride + c, weight<RB>(sb));
+            ua[0] += dir_x(i) * fa; ua[1] += dir_y(i) * fa; ua[2] += dir_z(i) * fa;
+            ub[0] += dir_x(i) * fb; ub[1] += dir_y(i) * fb; ub[2] += dir_z(i) * fb;
+        }
+        const double d0 = ua[0] - ub[0], d1 = ua[1] - ub[1], d2 = ua[2] - ub[2];
+        const double e2 = d0 * d0 + d1 * d1 + d2 * d2, r2 = ub[0] * ub[0] + ub[1] * ub[1] + ub[2] * ub[2];
+        mx = fmax(mx, sqrt(e2));
+        mr = fmax(mr, sqrt(r2));
+        se += e2;
+        sr += r2;
+        cnt += 1;
+    }
+    sh[0][threadIdx.x] = mx; sh[1][threadIdx.x] = se; sh[2][threadIdx.x] = sr; sh[3][threadIdx.x] = mr;
+    sh[4][threadIdx.x] = cnt;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            sh[0][threadIdx.x] = fmax(sh[0][threadIdx.x], sh[0][threadIdx.x + w]);
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+            sh[2][threadIdx.x] += sh[2][threadIdx.x + w];
+            sh[3][threadIdx.x] = fmax(sh[3][threadIdx.x], sh[3][threadIdx.x + w]);
+            sh[4][threadIdx.x] += sh[4][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 5) partial[blockIdx.x * 5 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_compare_final(const double *partial, int nblocks, double *out) {
+    if (threadIdx.x != 0) return;
+    double r[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < nblocks; b++) {
+        r[0] = fmax(r[0], partial[b * 5 + 0]);
+        r[1] += partial[b * 5 + 1];
+        r[2] += partial[b * 5 + 2];
+        r[3] = fmax(r[3], partial[b * 5 + 3]);
+        r[4] += partial[b * 5 + 4];
+    }
+    for (int q = 0; q < 5; q++) out[q] = r[q];
+}
+
 __global__ void k_reduce_final(const double *partial, int nblocks, double *out) {
     if (threadIdx.x >= 5) return;
     const int q = threadIdx.x;
@@ -691,6 +748,40 @@ int lbm_cu_reduce_conserved(lbm_lattice *l, int layout, double out[5], void *str
     }
     CU(cudaGetLastError());
     k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, res);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int layout_b, double out[5],
+                            void *stream) {
+    if (!a || !b || !out) return fail("NULL argument");
+    if (a->nx != b->nx || a->ny != b->ny || a->nz != b->nz) return fail("lattices differ in size");
+    const size_t need = (size_t)kRedBlocks * 5 * sizeof(double) + 8 * sizeof(double);
+    if (ensure_stage(a, need)) return -1;
+    double *partial = (double *)a->stage;
+    double *res = partial + (size_t)kRedBlocks * 5;
+    const int blocks = std::min<int64_t>(kRedBlocks, std::max<int64_t>(1, grid_for(a->n)));
+    cudaStream_t st = S(stream);
+#define CMP(SA_, SB_) k_compare<SA_, SB_><<<blocks, kBlock, 0, st>>>(a->h, layout_a & 1, b->h, layout_b & 1, partial)
+#define CMPB(SA_)                                   \
+    switch (b->storage) {                           \
+        case kF32: CMP(SA_, float); break;          \
+        case kF64: CMP(SA_, double); break;         \
+        case kF16: CMP(SA_, __half); break;         \
+        case kBF16: CMP(SA_, __nv_bfloat16); break; \
+    }
+    switch (a->storage) {
+        case kF32: CMPB(float); break;
+        case kF64: CMPB(double); break;
+        case kF16: CMPB(__half); break;
+        case kBF16: CMPB(__nv_bfloat16); break;
+    }
+#undef CMPB
+#undef CMP
+    CU(cudaGetLastError());
+    k_compare_final<<<1, 32, 0, st>>>(partial, blocks, res);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));

@@ -187,6 +187,7 @@ constexpr int kParamLattices = 8;
 struct StepArgs {
     LatDesc tab[kParamLattices];
     const LatDesc *dtab;
+    const int32_t *block_lattice;  // lattice of every block (device tables), or null
     int ntab;
     int store_v, store_rho;
 };
@@ -204,6 +205,9 @@ __device__ __forceinline__ const LatDesc &lattice_of(const StepArgs &a) {
         }
         return a.tab[li];
     }
+    // one load of a precomputed map instead of a binary search of dependent
+    // global loads at the start of every block
+    if (a.block_lattice) return a.dtab[a.block_lattice[blockIdx.x]];
     return a.dtab[find_lattice(a.dtab, a.ntab, blockIdx.x)];
 }
 
