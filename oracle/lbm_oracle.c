@@ -30,8 +30,13 @@
  * inserted into the reference BGK update in place of the constant inv_tau.
  *
  * The file is compiled once per storage variant (VARIANT = 0 f32, 1 f64,
- * 2 shifted f16, 3 shifted bf16).  Shifted variants store f_i - w_i and do
- * all arithmetic in float.
+ * 2 shifted f16, 3 shifted bf16).  Shifted variants store g_i = f_i - w_i
+ * and do all arithmetic in float, in deviation form: the same model with
+ * the operations the GB300 kernels perform for these types (pair sums,
+ * explicit fused multiply-adds via fmaf, see dev_* below).  The reference
+ * has no 16-bit storage, so for these variants this file is the definition
+ * the kernels are held to; the f32 and f64 variants are pinned to the
+ * reference itself.
  */
 #include <stdint.h>
 #include <string.h>
@@ -109,9 +114,13 @@ static inline uint16_t f_to_bf16(float f) {
 }
 #define LD(p, i) (bf16_to_f(p) + weight(i))
 #define STV(v, i) (f_to_bf16((v) - weight(i)))
+#define LDD(p) (bf16_to_f(p))
+#define STD(v) (f_to_bf16(v))
 #elif VARIANT == 2
 #define LD(p, i) ((REAL)(p) + weight(i))
 #define STV(v, i) ((STOR)((v) - weight(i)))
+#define LDD(p) ((REAL)(p))
+#define STD(v) ((STOR)(v))
 #else
 #define LD(p, i) (p)
 #define STV(v, i) (v)
@@ -249,6 +258,102 @@ static REAL gravity_chain(REAL rho, REAL gx, REAL gy, REAL gz, REAL t[9]) {
     return r;
 }
 
+#if SHIFTED
+/* ----------------------------------------------------------- deviation form
+ * Collision of the shifted types on the stored deviations g_i = f_i - w_i:
+ *   rho - 1 = sum g_i + CW,  j = sum e_i g_i,  u = j (incompressible form),
+ *   A = dd_param - 1 = (rho - 1) - 3/2 |u|^2,
+ *   f_i^eq - w_i = w_i (A + 3 e_i.u + 9/2 (e_i.u)^2),
+ *   g_i' = (1 - omega) g_i + omega (f_i^eq - w_i),
+ * per opposite pair (2k, 2k+1) as P +- Q, P = omega w (A + 9/2 s^2),
+ * Q = 3 omega w s, s = e_2k.u.  CW = sum of the float weights - 1 = 2^-26 and
+ * CP = 2 w18 + 8 w36 - (float)(1/3) = -2^-27 keep the float weights' exact
+ * offsets, so the model is the reference's one.  Subgrid rate:
+ *   Pi_ab = sum e_a e_b g + CP delta - (rho - 1)/3 delta - u_a u_b,
+ *   omega = 2 / (tau0 + sqrt(tau0^2 + C sqrt(Pi:Pi))).
+ * Every fmaf is a single-rounding fused multiply-add, as on the GPU. */
+#define CW 0x1p-26f
+#define CP (-0x1p-27f)
+
+static void dev_moments(const REAL g[19], REAL *dl, REAL *jx, REAL *jy, REAL *jz, REAL m2[6]) {
+    REAL s[9], t[9];
+    for (int k = 0; k < 9; k++) {
+        s[k] = g[2 * k] + g[2 * k + 1];
+        t[k] = g[2 * k] - g[2 * k + 1];
+    }
+    REAL a23 = s[2] + s[3], a45 = s[4] + s[5], a67 = s[6] + s[7];
+    *dl = ((((s[0] + s[1]) + a23) + (a45 + a67)) + (s[8] + g[18])) + CW;
+    *jx = ((t[0] + t[2]) + (t[3] + t[4])) + t[5];
+    *jy = ((t[1] + t[2]) - t[3]) + (t[6] + t[7]);
+    *jz = ((t[4] - t[5]) + (t[6] - t[7])) + t[8];
+    m2[0] = (s[0] + a23) + a45;
+    m2[1] = (s[1] + a23) + a67;
+    m2[2] = (s[8] + a45) + a67;
+    m2[3] = s[2] - s[3];
+    m2[4] = s[4] - s[5];
+    m2[5] = s[6] - s[7];
+}
+
+static void dev_pair(REAL g[19], int k, REAL v, REAL a, REAL b, REAL A, REAL om1) {
+    REAL h = fmaf(K45 * v, v, A);
+    REAL P = a * h, Q = b * v;
+    g[2 * k] = fmaf(om1, g[2 * k], P + Q);
+    g[2 * k + 1] = fmaf(om1, g[2 * k + 1], P - Q);
+}
+
+static void dev_relax(REAL g[19], REAL om, REAL A, REAL vx, REAL vy, REAL vz) {
+    REAL om1 = (REAL)1.0f - om;
+    REAL a18 = om * C18, a36 = om * C36, a3 = om * C3;
+    REAL b18 = K3 * a18, b36 = K3 * a36;
+    dev_pair(g, 0, vx, a18, b18, A, om1);
+    dev_pair(g, 1, vy, a18, b18, A, om1);
+    dev_pair(g, 2, vx + vy, a36, b36, A, om1);
+    dev_pair(g, 3, vx - vy, a36, b36, A, om1);
+    dev_pair(g, 4, vx + vz, a36, b36, A, om1);
+    dev_pair(g, 5, vx - vz, a36, b36, A, om1);
+    dev_pair(g, 6, vy + vz, a36, b36, A, om1);
+    dev_pair(g, 7, vy - vz, a36, b36, A, om1);
+    dev_pair(g, 8, vz, a18, b18, A, om1);
+    g[18] = fmaf(om1, g[18], a3 * A);
+}
+
+static void dev_equilibria(REAL vx, REAL vy, REAL vz, REAL A, REAL g[19]) {
+    REAL b18 = K3 * C18, b36 = K3 * C36;
+    REAL v[9] = {vx, vy, vx + vy, vx - vy, vx + vz, vx - vz, vy + vz, vy - vz, vz};
+    for (int k = 0; k < 9; k++) {
+        int axis = k < 2 || k == 8;
+        REAL h = fmaf(K45 * v[k], v[k], A);
+        REAL P = (axis ? C18 : C36) * h, Q = (axis ? b18 : b36) * v[k];
+        g[2 * k] = P + Q;
+        g[2 * k + 1] = P - Q;
+    }
+    g[18] = C3 * A;
+}
+
+static void dev_collide(REAL g[19], REAL dl, REAL vx, REAL vy, REAL vz, const REAL m2[6], REAL A, REAL inv_tau,
+                        REAL tau0, REAL les_c) {
+    REAL om = inv_tau;
+    if (les_c != (REAL)0) {
+        REAL pxx = fmaf(-vx, vx, fmaf(-C3, dl, m2[0] + CP));
+        REAL pyy = fmaf(-vy, vy, fmaf(-C3, dl, m2[1] + CP));
+        REAL pzz = fmaf(-vz, vz, fmaf(-C3, dl, m2[2] + CP));
+        REAL pxy = fmaf(-vx, vy, m2[3]);
+        REAL pxz = fmaf(-vx, vz, m2[4]);
+        REAL pyz = fmaf(-vy, vz, m2[5]);
+        REAL off = fmaf(pyz, pyz, fmaf(pxz, pxz, pxy * pxy));
+        REAL dia = fmaf(pzz, pzz, fmaf(pyy, pyy, pxx * pxx));
+        REAL q = fmaf((REAL)2.0f, off, dia);
+        om = (REAL)2.0f / (tau0 + sqrtf(fmaf(les_c, sqrtf(q), tau0 * tau0)));
+    }
+    dev_relax(g, om, A, vx, vy, vz);
+}
+
+static REAL dev_dp1(REAL vx, REAL vy, REAL vz, REAL dl) {
+    REAL u2 = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+    return fmaf(-K15, u2, dl);
+}
+#endif
+
 /* ------------------------------------------------------------------- init */
 /* lbm_init.cl:32-237: flags from the six face conditions (x faces win over
  * y faces, y over z), populations at rest equilibrium rho = 1, u = 0 in
@@ -285,6 +390,40 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
     for (int64_t c = 0; c < n; c++) {
         int32_t fl = flags[c];
         if (fl == FL_GHOST) continue; /* lbm_alpha.cl:31-32 */
+#if SHIFTED
+        {
+            REAL g[19], m2[6], dl, vx, vy, vz, r, t[9];
+            int write = 0;
+            for (int i = 0; i < 19; i++) g[i] = LDD(dd[i * n + c]);
+            dev_moments(g, &dl, &vx, &vy, &vz, m2);
+            r = (REAL)1.0f + dl;
+            if (fl == FL_FLUID) {
+                REAL A = dev_dp1(vx, vy, vz, dl);
+                dev_collide(g, dl, vx, vy, vz, m2, A, inv_tau, tau0, les_c);
+                r = gravity_chain(r, gx, gy, gz, t);
+                write = 1;
+            } else if (fl == FL_OBSTACLE) {
+                vx = 0; vy = 0; vz = 0;
+            } else if (fl == FL_LID) {
+                vx = lid; vy = 0; vz = 0;
+                REAL A = -K15 * (vx * vx);
+                dev_equilibria(vx, vy, vz, A, g);
+                r = gravity_chain((REAL)1.0f, gx, gy, gz, t);
+                write = 1;
+            }
+            if (write) {
+                if (gx != 0 || gy != 0 || gz != 0)
+                    for (int k = 0; k < 9; k++) {
+                        g[2 * k + 1] -= t[k];
+                        g[2 * k] += t[k];
+                    }
+                for (int i = 0; i < 19; i++) dd[opp(i) * n + c] = STD(g[i]);
+            }
+            if (store_vel) { vel[c] = vx; vel[n + c] = vy; vel[2 * n + c] = vz; }
+            if (store_rho) rho[c] = r;
+            continue;
+        }
+#endif
         REAL f[19];
         for (int i = 0; i < 19; i++) f[i] = LD(dd[i * n + c], i);
         /* moments in the order of lbm_alpha.cl:61-156 */
@@ -358,6 +497,36 @@ void SFX(orc_beta)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_t
             src[i] = nbr(&g, c, -EX[i], -EY[i], -EZ[i]);
             dst[i] = nbr(&g, c, EX[i], EY[i], EZ[i]);
         }
+#if SHIFTED
+        {
+            REAL g[19], m2[6], dl, vx, vy, vz, r;
+            for (int i = 0; i < 19; i++) g[i] = LDD(dd[opp(i) * n + src[i]]);
+            dev_moments(g, &dl, &vx, &vy, &vz, m2);
+            r = (REAL)1.0f + dl;
+            if (fl == FL_FLUID) {
+                REAL A = dev_dp1(vx, vy, vz, dl);
+                dev_collide(g, dl, vx, vy, vz, m2, A, inv_tau, tau0, les_c);
+                r = (REAL)1.0f + A;
+            } else if (fl == FL_OBSTACLE) {
+                vx = 0; vy = 0; vz = 0;
+                for (int k = 0; k < 9; k++) {
+                    REAL tmp = g[2 * k + 1];
+                    g[2 * k + 1] = g[2 * k];
+                    g[2 * k] = tmp;
+                }
+            } else if (fl == FL_LID) {
+                vx = lid; vy = 0; vz = 0;
+                REAL A = -K15 * (vx * vx);
+                dev_equilibria(vx, vy, vz, A, g);
+                r = (REAL)1.0f + A;
+            }
+            for (int i = 0; i < 19; i++) dd[i * n + dst[i]] = STD(g[i]);
+            if (fl == FL_GHOST) continue;
+            if (store_vel) { vel[c] = vx; vel[n + c] = vy; vel[2 * n + c] = vz; }
+            if (store_rho) rho[c] = r;
+            continue;
+        }
+#endif
         for (int i = 0; i < 19; i++) f[i] = LD(dd[opp(i) * n + src[i]], i);
         /* moments in the order of lbm_beta.cl:261-483 */
         REAL r, vx, vy, vz;

@@ -207,6 +207,47 @@ def test_subgrid_collision_matches_formula(oracle_mod, storage, tol):
     assert rel.max() < tol
 
 
+def _stored_deviation(dd, storage):
+    """The stored g_i = f_i - w_i of a shifted lattice, exactly, as float64."""
+    if storage == "bf16":
+        return (dd.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    return dd.astype(np.float64)
+
+
+def _ulp16(x, storage):
+    """Spacing of the 16-bit type at x (half precision has subnormals below 2^-14)."""
+    mant, emin = (10, -14) if storage == "f16" else (7, -126)
+    e = np.maximum(np.floor(np.log2(np.maximum(np.abs(x), 2.0 ** -140))), emin)
+    return 2.0 ** (e - mant)
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("cs", [0.0, 0.17])
+def test_deviation_form_collision_matches_formula(oracle_mod, storage, cs):
+    """The shifted types collide on deviations with fused multiply-adds; the
+    result must be the float64 model of the reference (float weights, the
+    incompressible equilibrium, the Smagorinsky rate) up to the rounding of
+    the stored value: within one unit in the last place of the 16-bit type."""
+    O = oracle_mod
+    dims = (10, 9, 8)
+    tau0 = O.cavity_tau(0.1, 64, 20000.0)
+    p = O.Params.lattice(tau0, 0.0, cs=cs, dtype=np.float32)
+    s = O.Solver(O.OracleKernels(storage), dims, [O.FLAG_OBSTACLE] * 6, p, storage)
+    s.k.perturb(s.lat, (0, 0, 0), dims, 99, 5e-2)
+    s.step()
+    m = s.lat.flags == O.FLAG_FLUID
+    w = np.array([np.float32(1 / 18)] * 4 + [np.float32(1 / 36)] * 12 + [np.float32(1 / 18)] * 2
+                 + [np.float32(1 / 3)], dtype=np.float64)[:, None]
+    f0 = _stored_deviation(s.lat.dd[:, m], storage) + w
+    s.step()
+    got = _stored_deviation(s.lat.dd[:, m][O.OPP], storage)
+    if cs:
+        want = _np_les_alpha(f0, float(np.float32(tau0)), float(np.float32(O.les_coefficient(cs)))) - w
+    else:
+        want = _np_les_alpha(f0, float(np.float32(tau0)), 0.0) - w
+    assert np.all(np.abs(got - want) <= _ulp16(want, storage))
+
+
 def test_subgrid_model_off_at_equilibrium(oracle_mod):
     """At equilibrium Pi^neq vanishes, so tau_eff = tau0: one LES step equals
     one plain BGK step with inv_tau = 1/tau0.  The seeded start-up stores

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -27,20 +28,20 @@ using namespace lbm_rt;
 namespace lbm_rt {
 
 template <typename S, bool PAIR>
-int launch_tick_t(bool les, const StepArgs &a, int blocks, int j, cudaStream_t st) {
+int launch_tick_t(bool les, const BatchArgs &a, int blocks, int j, cudaStream_t st) {
     if (blocks <= 0) return 0;
     if constexpr (PAIR) {
-        if (les) k_step2<S, true, false><<<blocks, kBlock, 0, st>>>(a, j);
-        else k_step2<S, false, false><<<blocks, kBlock, 0, st>>>(a, j);
+        if (les) k_step2<S, true><<<blocks, kBlock, 0, st>>>(a, j);
+        else k_step2<S, false><<<blocks, kBlock, 0, st>>>(a, j);
     } else {
-        if (les) k_step<S, true, false><<<blocks, kBlock, 0, st>>>(a, j);
-        else k_step<S, false, false><<<blocks, kBlock, 0, st>>>(a, j);
+        if (les) k_step<S, true><<<blocks, kBlock, 0, st>>>(a, j);
+        else k_step<S, false><<<blocks, kBlock, 0, st>>>(a, j);
     }
     CU(cudaGetLastError());
     return 0;
 }
 
-int launch_tick(int storage, bool pair, bool les, const StepArgs &a, int blocks, int j, cudaStream_t st) {
+int launch_tick(int storage, bool pair, bool les, const BatchArgs &a, int blocks, int j, cudaStream_t st) {
     if (pair) {
         switch (storage) {
             case kF32: return launch_tick_t<float, true>(les, a, blocks, j, st);
@@ -115,15 +116,18 @@ struct Ensemble {
         bool active = false;
         int64_t id = -1;
     };
+    // One launch per chunk of up to kBatchLattices members per step.
+    struct Chunk {
+        std::unique_ptr<BatchArgs> args;  // descriptors with this tick's parities
+        int blocks = 0;
+        bool les = false;
+    };
     struct Group {
         int storage = 0;
-        bool pair = false, les = false;
+        bool pair = false;
         std::vector<int> members;
-        std::vector<LatDesc> htab;
-        LatDesc *dtab = nullptr;
-        int32_t *dmap = nullptr;  // lattice index of every block
-        size_t cap = 0;
-        int blocks = 0;
+        std::vector<Chunk> chunks;
+        int32_t *dmap = nullptr;  // lattice index (within its chunk) of every block
     };
     std::vector<Slot> slots;
     std::vector<Group> groups;
@@ -131,15 +135,13 @@ struct Ensemble {
     int shape = 1;
     bool dirty = true;
     cudaGraphExec_t graph = nullptr;
+    std::vector<int> graph_parity;  // parities baked into the captured graph
     cudaStream_t cap = nullptr;
 
     ~Ensemble() {
         drop_graph();
         if (cap) cudaStreamDestroy(cap);
-        for (auto &g : groups) {
-            if (g.dtab) cudaFree(g.dtab);
-            if (g.dmap) cudaFree(g.dmap);
-        }
+        free_groups();
         for (auto &s : slots)
             if (s.lat) lbm_cu_destroy(s.lat);
     }
@@ -147,14 +149,16 @@ struct Ensemble {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
     }
-
-    // Descriptor tables of the active cavities, one group per (storage, shape).
-    int build_groups() {
-        for (auto &g : groups) {
-            if (g.dtab) cudaFree(g.dtab);
+    void free_groups() {
+        for (auto &g : groups)
             if (g.dmap) cudaFree(g.dmap);
-        }
         groups.clear();
+    }
+
+    // Member groups of the active cavities, one per (storage, shape), and
+    // their block maps.
+    int build_groups() {
+        free_groups();
         for (size_t i = 0; i < slots.size(); i++) {
             const Slot &s = slots[i];
             if (!s.active) continue;
@@ -171,57 +175,66 @@ struct Ensemble {
             g->members.push_back((int)i);
         }
         for (auto &g : groups) {
-            g.cap = g.members.size();
-            CU(cudaMalloc((void **)&g.dtab, g.cap * sizeof(LatDesc)));
             const int per = cells_per_block(g.pair);
             std::vector<int32_t> map;
             for (size_t k = 0; k < g.members.size(); k++) {
                 const int64_t n = slots[g.members[k]].lat->n;
-                map.insert(map.end(), (size_t)((n + per - 1) / per), (int32_t)k);
+                map.insert(map.end(), (size_t)((n + per - 1) / per), (int32_t)(k % kBatchLattices));
             }
             CU(cudaMalloc((void **)&g.dmap, map.size() * sizeof(int32_t)));
             CU(cudaMemcpy(g.dmap, map.data(), map.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+            g.chunks.resize((g.members.size() + kBatchLattices - 1) / kBatchLattices);
+            for (auto &c : g.chunks) c.args.reset(new BatchArgs());
         }
         dirty = false;
         drop_graph();
         return refresh_tables();
     }
 
-    // Step-counter parities (and block numbering) into the device tables.
+    // Descriptors with the current step-counter parities (and block
+    // numbering) into the launch arguments; a graph captured with other
+    // parities is dropped.
     int refresh_tables() {
+        std::vector<int> parity;
         for (auto &g : groups) {
-            g.htab.clear();
-            g.les = false;
-            int first = 0;
             const int per = cells_per_block(g.pair);
-            for (int i : g.members) {
-                LatDesc h = slots[i].lat->h;
-                h.first_block = first;
-                h.nblocks = (int)((h.n + per - 1) / per);
-                h.parity = (int)(slots[i].done & 1);
-                first += h.nblocks;
-                if (uses_les(h)) g.les = true;
-                g.htab.push_back(h);
+            int64_t map_off = 0;
+            for (size_t c = 0; c < g.chunks.size(); c++) {
+                Chunk &ch = g.chunks[c];
+                BatchArgs &a = *ch.args;
+                memset(&a, 0, sizeof(a));
+                const size_t k0 = c * kBatchLattices, k1 = std::min(g.members.size(), k0 + kBatchLattices);
+                int first = 0;
+                ch.les = false;
+                for (size_t k = k0; k < k1; k++) {
+                    const Slot &s = slots[g.members[k]];
+                    LatDesc h = s.lat->h;
+                    h.first_block = first;
+                    h.nblocks = (int)((h.n + per - 1) / per);
+                    h.parity = (int)(s.done & 1);
+                    first += h.nblocks;
+                    if (uses_les(h)) ch.les = true;
+                    a.tab[k - k0] = h;
+                    parity.push_back(h.parity);
+                }
+                a.ntab = (int)(k1 - k0);
+                a.block_lattice = g.dmap + map_off;
+                ch.blocks = first;
+                map_off += first;
             }
-            g.blocks = first;
-            CU(cudaMemcpy(g.dtab, g.htab.data(), g.htab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice));
         }
+        if (parity != graph_parity) drop_graph();
+        graph_parity = parity;
         return 0;
     }
 
     int launch_all(int j, bool store, cudaStream_t st) {
-        for (auto &g : groups) {
-            StepArgs a;
-            memset(&a, 0, sizeof(a));
-            a.ntab = (int)g.htab.size();
-            a.dtab = g.dtab;
-            a.block_lattice = g.dmap;
-            a.store_v = store ? store_v : 0;
-            a.store_rho = 0;
-            // the tick kernels always read the device table, so a captured
-            // graph stays valid while parities change between ticks
-            if (launch_tick(g.storage, g.pair, g.les, a, g.blocks, j, st)) return -1;
-        }
+        for (auto &g : groups)
+            for (auto &ch : g.chunks) {
+                ch.args->store_v = store ? store_v : 0;
+                ch.args->store_rho = 0;
+                if (launch_tick(g.storage, g.pair, ch.les, *ch.args, ch.blocks, j, st)) return -1;
+            }
         return 0;
     }
 

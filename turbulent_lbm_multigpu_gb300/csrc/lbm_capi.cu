@@ -396,24 +396,16 @@ __global__ void k_reduce_final(const double *partial, int nblocks, double *out) 
 
 // ------------------------------------------------------------- dispatchers
 template <typename S, bool PAIR>
-int launch_step_t(int parity, bool les, const StepArgs &a, int blocks, cudaStream_t st) {
+int launch_step_t(int parity, bool les, const DomainArgs &a, int blocks, cudaStream_t st) {
     if (blocks <= 0) return 0;
-    const bool pt = a.ntab <= kParamLattices;
-#define STEP(K_, L_, P_) K_<S, L_, P_><<<blocks, kBlock, 0, st>>>(a)
-#define STEPS(KA_, KB_)                                                                   \
-    if (parity) {                                                                         \
-        if (les) { if (pt) STEP(KA_, true, true); else STEP(KA_, true, false); }          \
-        else { if (pt) STEP(KA_, false, true); else STEP(KA_, false, false); }            \
-    } else {                                                                              \
-        if (les) { if (pt) STEP(KB_, true, true); else STEP(KB_, true, false); }          \
-        else { if (pt) STEP(KB_, false, true); else STEP(KB_, false, false); }            \
-    }
+#define STEP(K_, L_) K_<S, L_><<<blocks, kBlock, 0, st>>>(a)
     if constexpr (PAIR) {
-        STEPS(k_alpha2, k_beta2)
+        if (parity) { if (les) STEP(k_alpha2, true); else STEP(k_alpha2, false); }
+        else { if (les) STEP(k_beta2, true); else STEP(k_beta2, false); }
     } else {
-        STEPS(k_alpha, k_beta)
+        if (parity) { if (les) STEP(k_alpha, true); else STEP(k_alpha, false); }
+        else { if (les) STEP(k_beta, true); else STEP(k_beta, false); }
     }
-#undef STEPS
 #undef STEP
     CU(cudaGetLastError());
     return 0;
@@ -428,19 +420,8 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab) {
     return true;
 }
 
-// One step over `ntab` lattices.  `htab` holds the host copy of the
-// descriptors with first_block/nblocks for the launch shape; the launch uses
-// it as kernel parameters when it fits, else the device copy `dtab`.
-int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab,
-                int blocks, int sv, int sr, cudaStream_t st) {
-    StepArgs a;
-    memset(&a, 0, sizeof(a));
-    a.ntab = ntab;
-    a.dtab = dtab;
-    a.store_v = sv;
-    a.store_rho = sr;
-    if (ntab <= kParamLattices)
-        for (int i = 0; i < ntab; i++) a.tab[i] = htab[i];
+static int launch_chunk(int storage, bool pair, int parity, bool les, const DomainArgs &a, int blocks,
+                        cudaStream_t st) {
     if (pair) {
         switch (storage) {
             case kF32: return launch_step_t<float, true>(parity, les, a, blocks, st);
@@ -456,6 +437,27 @@ int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *hta
         case kBF16: return launch_step_t<__nv_bfloat16, false>(parity, les, a, blocks, st);
     }
     return fail("unknown storage type");
+}
+
+// One step over `ntab` lattices of one storage type, kParamLattices per
+// launch.  `htab` holds the descriptors with nblocks for the launch shape.
+int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
+                cudaStream_t st) {
+    for (int c0 = 0; c0 < ntab; c0 += kParamLattices) {
+        DomainArgs a;
+        memset(&a, 0, sizeof(a));
+        a.ntab = std::min(kParamLattices, ntab - c0);
+        a.store_v = sv;
+        a.store_rho = sr;
+        int blocks = 0;
+        for (int i = 0; i < a.ntab; i++) {
+            a.tab[i] = htab[c0 + i];
+            a.tab[i].first_block = blocks;
+            blocks += a.tab[i].nblocks;
+        }
+        if (launch_chunk(storage, pair, parity, les, a, blocks, st)) return -1;
+    }
+    return 0;
 }
 
 Box make_box(const lbm_lattice *l, const int o[3], const int s[3]) {
@@ -623,8 +625,7 @@ int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
     const bool pair = l->allow_pair && pair_shape(l->storage, &h, 1);
     h.first_block = 0;
     h.nblocks = (int)((l->n + cells_per_block(pair) - 1) / cells_per_block(pair));
-    return launch_step(l->storage, pair, parity & 1, uses_les(h), &h, nullptr, 1, h.nblocks, l->store_v, l->store_rho,
-                       S(stream));
+    return launch_step(l->storage, pair, parity & 1, uses_les(h), &h, 1, l->store_v, l->store_rho, S(stream));
 }
 
 static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], void *host, const int norm[3],
@@ -867,9 +868,7 @@ struct lbm_domain {
     std::vector<std::vector<CommGeom>> comms;
     std::vector<std::vector<int>> bc;
     std::vector<int> coords;  // 3 per subdomain
-    LatDesc *d_tab[2] = {nullptr, nullptr};  // [one-cell, two-cell] block numbering
-    std::vector<LatDesc> h_tab[2];
-    int blocks[2] = {0, 0};
+    std::vector<LatDesc> h_tab[2];  // [one-cell, two-cell] block counts
     bool pair = false;
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
@@ -944,24 +943,19 @@ int domain_build_plans(lbm_domain *D) {
 }
 
 int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
+    (void)st;
     if (!D->tab_dirty) return 0;
     for (int shape = 0; shape < 2; shape++) {
         std::vector<LatDesc> tab;
-        int first = 0;
         const int per = cells_per_block(shape == 1);
         for (auto *l : D->subs) {
             LatDesc h = l->h;
-            h.first_block = first;
             h.nblocks = (int)((l->n + per - 1) / per);
-            first += h.nblocks;
             tab.push_back(h);
         }
-        D->blocks[shape] = first;
         D->h_tab[shape] = tab;
-        CU(cudaMemcpyAsync(D->d_tab[shape], tab.data(), tab.size() * sizeof(LatDesc), cudaMemcpyHostToDevice, st));
     }
     D->pair = D->allow_pair && pair_shape(D->storage, D->h_tab[1].data(), (int)D->subs.size());
-    CU(cudaStreamSynchronize(st));
     D->tab_dirty = false;
     return 0;
 }
@@ -983,8 +977,7 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (timed && domain_record(D, st, &e0)) return -1;
     const int sh = D->pair ? 1 : 0;
-    if (launch_step(D->storage, D->pair, parity, les, D->h_tab[sh].data(), D->d_tab[sh], (int)D->subs.size(),
-                    D->blocks[sh], sv, sr, st))
+    if (launch_step(D->storage, D->pair, parity, les, D->h_tab[sh].data(), (int)D->subs.size(), sv, sr, st))
         return -1;
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
@@ -1057,11 +1050,6 @@ int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int 
         D->bc.push_back(bc);
         D->comms.push_back(cms);
     }
-    for (int shape = 0; shape < 2; shape++)
-        if (cudaMalloc((void **)&D->d_tab[shape], nsub * sizeof(LatDesc)) != cudaSuccess) {
-            lbm_cu_domain_destroy(D);
-            return fail("cudaMalloc of the subdomain table failed");
-        }
     if (domain_build_plans(D)) {
         std::string m = g_err;
         lbm_cu_domain_destroy(D);
@@ -1077,8 +1065,6 @@ int lbm_cu_domain_destroy(lbm_domain *D) {
     if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
     for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
     for (auto *l : D->subs) lbm_cu_destroy(l);
-    for (int shape = 0; shape < 2; shape++)
-        if (D->d_tab[shape]) cudaFree(D->d_tab[shape]);
     for (int p = 0; p < 2; p++)
         for (int a = 0; a < 3; a++)
             if (D->d_plan[p][a]) cudaFree(D->d_plan[p][a]);

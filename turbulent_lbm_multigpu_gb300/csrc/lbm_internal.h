@@ -39,11 +39,11 @@ inline bool uses_les(const LatDesc &h) { return h.pd[P_LES] != 0.0; }
 bool pair_shape(int storage, const LatDesc *tab, int ntab);
 inline int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
 
-// One step over `ntab` lattices of one storage type; `htab` holds the
-// descriptors with first_block/nblocks for the launch shape, used as
-// kernel parameters when they fit, else the device copy `dtab`.
-int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, const LatDesc *dtab, int ntab,
-                int blocks, int sv, int sr, cudaStream_t st);
+// One step over `ntab` lattices of one storage type, kParamLattices
+// descriptors per launch; `htab` holds the descriptors with nblocks for the
+// launch shape.
+int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
+                cudaStream_t st);
 }  // namespace lbm_rt
 
 struct lbm_lattice {

@@ -13,9 +13,13 @@
 // the writing thread itself, so both kernels update the buffer in place with
 // no synchronisation.
 //
-// Arithmetic follows the reference kernels operation by operation.  This file
-// is compiled with -fmad=false and IEEE division/square root, which makes the
-// results bit-identical to the reference kernel source run on a CPU.
+// For float and double storage the arithmetic follows the reference kernels
+// operation by operation.  This file is compiled with -fmad=false and IEEE
+// division/square root, which makes those results bit-identical to the
+// reference kernel source run on a CPU.  The shifted 16-bit storage types
+// (which the reference does not have) compute the same model in deviation
+// form with explicit fused multiply-adds (see "deviation form" below); the
+// CPU oracle states that arithmetic with fmaf, so it is bit-exact as well.
 //
 // Two kernel shapes:
 //   k_beta / k_alpha    one cell per thread, any storage and size;
@@ -82,11 +86,23 @@ __device__ __forceinline__ P2 msqrt(P2 x) { return P2{sqrtf(x.x), sqrtf(x.y)}; }
 __device__ __forceinline__ float mrcp(float x) { return 1.0f / x; }
 __device__ __forceinline__ double mrcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ P2 mrcp(P2 x) { return P2{1.0f / x.x, 1.0f / x.y}; }
+// a * b + c rounded once (IEEE fused multiply-add)
+__device__ __forceinline__ float mfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ P2 mfma(P2 a, P2 b, P2 c) {
+    return P2{__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y)};
+}
+__device__ __forceinline__ float mdiv(float a, float b) { return a / b; }
+__device__ __forceinline__ P2 mdiv(P2 a, P2 b) { return P2{a.x / b.x, a.y / b.y}; }
 
 // ---------------------------------------------------------------- storage
 template <typename S> struct Store;
+// ld/st convert between stored values and full populations f_i (used by
+// init, start-up, box IO and reductions).  The step kernels of the shifted
+// types move the stored deviations g_i = f_i - w_i without shifting (dld /
+// dst), because their collision works on deviations (kDev).
 template <> struct Store<float> {
     using R = float;
+    static constexpr bool kDev = false;
     __device__ static __forceinline__ R ld(const float *p, R) { return *p; }
     __device__ static __forceinline__ void st(float *p, R v, R) { *p = v; }
     __device__ static __forceinline__ P2 ld2(const float *p, R) {
@@ -97,11 +113,20 @@ template <> struct Store<float> {
 };
 template <> struct Store<double> {
     using R = double;
+    static constexpr bool kDev = false;
     __device__ static __forceinline__ R ld(const double *p, R) { return *p; }
     __device__ static __forceinline__ void st(double *p, R v, R) { *p = v; }
 };
 template <> struct Store<__half> {
     using R = float;
+    static constexpr bool kDev = true;
+    __device__ static __forceinline__ R dld(const __half *p) { return __half2float(*p); }
+    __device__ static __forceinline__ void dst(__half *p, R v) { *p = __float2half_rn(v); }
+    __device__ static __forceinline__ P2 dld2(const __half *p) {
+        const float2 v = __half22float2(*(const __half2 *)p);
+        return P2{v.x, v.y};
+    }
+    __device__ static __forceinline__ void dst2(__half *p, P2 v) { *(__half2 *)p = __floats2half2_rn(v.x, v.y); }
     __device__ static __forceinline__ R ld(const __half *p, R w) { return __half2float(*p) + w; }
     __device__ static __forceinline__ void st(__half *p, R v, R w) { *p = __float2half_rn(v - w); }
     __device__ static __forceinline__ P2 ld2(const __half *p, R w) {
@@ -115,6 +140,16 @@ template <> struct Store<__half> {
 };
 template <> struct Store<__nv_bfloat16> {
     using R = float;
+    static constexpr bool kDev = true;
+    __device__ static __forceinline__ R dld(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+    __device__ static __forceinline__ void dst(__nv_bfloat16 *p, R v) { *p = __float2bfloat16_rn(v); }
+    __device__ static __forceinline__ P2 dld2(const __nv_bfloat16 *p) {
+        const float2 v = __bfloat1622float2(*(const __nv_bfloat162 *)p);
+        return P2{v.x, v.y};
+    }
+    __device__ static __forceinline__ void dst2(__nv_bfloat16 *p, P2 v) {
+        *(__nv_bfloat162 *)p = __floats2bfloat162_rn(v.x, v.y);
+    }
     __device__ static __forceinline__ R ld(const __nv_bfloat16 *p, R w) { return __bfloat162float(*p) + w; }
     __device__ static __forceinline__ void st(__nv_bfloat16 *p, R v, R w) { *p = __float2bfloat16_rn(v - w); }
     __device__ static __forceinline__ P2 ld2(const __nv_bfloat16 *p, R w) {
@@ -139,6 +174,27 @@ template <typename R> struct K {
 };
 template <typename R> __host__ __device__ constexpr R weight(int i) {
     return i == 18 ? K<R>::c3 : (i < 4 || i >= 16) ? K<R>::c18 : K<R>::c36;
+}
+
+// What the step kernels hold per population: f_i (float/double storage) or
+// g_i = f_i - w_i (shifted 16-bit storage).
+template <typename S> __device__ __forceinline__ typename Store<S>::R pop_ld(const S *p, int i) {
+    using R = typename Store<S>::R;
+    if constexpr (Store<S>::kDev) return Store<S>::dld(p);
+    else return Store<S>::ld(p, weight<R>(i));
+}
+template <typename S> __device__ __forceinline__ void pop_st(S *p, typename Store<S>::R v, int i) {
+    using R = typename Store<S>::R;
+    if constexpr (Store<S>::kDev) Store<S>::dst(p, v);
+    else Store<S>::st(p, v, weight<R>(i));
+}
+template <typename S> __device__ __forceinline__ P2 pop_ld2(const S *p, int i) {
+    if constexpr (Store<S>::kDev) return Store<S>::dld2(p);
+    else return Store<S>::ld2(p, weight<float>(i));
+}
+template <typename S> __device__ __forceinline__ void pop_st2(S *p, P2 v, int i) {
+    if constexpr (Store<S>::kDev) Store<S>::dst2(p, v);
+    else Store<S>::st2(p, v, weight<float>(i));
 }
 
 // ---------------------------------------------------------- lattice table
@@ -169,46 +225,39 @@ template <typename M> __device__ __forceinline__ M parm(const LatDesc &d, int i)
     return Bc<M>::of(par<typename Scalar<M>::T>(d, i));
 }
 
-// Lattice of a block in a batched launch: binary search on first_block.
-__device__ __forceinline__ int find_lattice(const LatDesc *tab, int ntab, int block) {
-    int lo = 0, hi = ntab - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (tab[mid].first_block <= block) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Arguments of a step launch.  Up to kParamLattices descriptors travel in
-// the kernel parameter space (constant bank: block-uniform values stay in
-// uniform registers); larger batches use a device table.  first_block and
-// nblocks count blocks of the launched kernel shape.
+// Arguments of a step launch: the descriptors of all lattices it covers
+// travel in the kernel parameter space (the constant bank, so block-uniform
+// fields are read in place or re-read instead of held in registers).
+// Domains and single lattices launch up to kParamLattices per launch; the
+// batched tick kernels take up to kBatchLattices (the 32 KB parameter
+// space), larger ensembles launch once per chunk.  first_block and nblocks
+// count blocks of the launched kernel shape from the start of the launch.
 constexpr int kParamLattices = 8;
-struct StepArgs {
-    LatDesc tab[kParamLattices];
-    const LatDesc *dtab;
-    const int32_t *block_lattice;  // lattice of every block (device tables), or null
+constexpr int kBatchLattices = 112;
+template <int N> struct StepArgs {
+    LatDesc tab[N];
+    const int32_t *block_lattice;  // lattice of every block of the launch, or null
     int ntab;
     int store_v, store_rho;
 };
+using DomainArgs = StepArgs<kParamLattices>;
+using BatchArgs = StepArgs<kBatchLattices>;
 
-template <bool PT>
-__device__ __forceinline__ const LatDesc &lattice_of(const StepArgs &a) {
-    if (PT) {
-        int li = 0;
-        if (a.ntab > 1) {
-            int hi = a.ntab - 1;
-            while (li < hi) {
-                const int mid = (li + hi + 1) >> 1;
-                if (a.tab[mid].first_block <= (int)blockIdx.x) li = mid; else hi = mid - 1;
-            }
+// Lattice of this block: one load from the block map, else a binary search
+// on first_block.
+template <int N>
+__device__ __forceinline__ const LatDesc &lattice_of(const StepArgs<N> &a) {
+    int li = 0;
+    if (a.block_lattice) {
+        li = a.block_lattice[blockIdx.x];
+    } else if (a.ntab > 1) {
+        int hi = a.ntab - 1;
+        while (li < hi) {
+            const int mid = (li + hi + 1) >> 1;
+            if (a.tab[mid].first_block <= (int)blockIdx.x) li = mid; else hi = mid - 1;
         }
-        return a.tab[li];
     }
-    // one load of a precomputed map instead of a binary search of dependent
-    // global loads at the start of every block
-    if (a.block_lattice) return a.dtab[a.block_lattice[blockIdx.x]];
-    return a.dtab[find_lattice(a.dtab, a.ntab, blockIdx.x)];
+    return a.tab[li];
 }
 
 // ------------------------------------------------------------- equilibria
@@ -409,6 +458,200 @@ __device__ __forceinline__ bool alpha_case(int fl, M f[19], M &r, M &vx, M &vy, 
     return true;
 }
 
+// ---------------------------------------------------------- deviation form
+// The shifted 16-bit types hold g_i = f_i - w_i.  Their collision is the
+// same incompressible BGK / Smagorinsky model as above, written on the
+// deviations so that no population is shifted back and forth and the
+// multiply-adds fuse (every fmaf below is one IEEE fused multiply-add; the
+// oracle states the same operations in the same order):
+//   rho - 1 = sum_i g_i + kCW,  j = sum_i e_i g_i  (sum_i e_i w_i = 0),
+//   A = dd_param - 1 = (rho - 1) - 3/2 |u|^2  (u = j, as in the reference),
+//   f_i^eq - w_i = w_i (A + 3 e_i.u + 9/2 (e_i.u)^2),
+//   g_i' = (1 - omega) g_i + omega (f_i^eq - w_i),
+// taken per opposite pair (2k, 2k+1) as P +- Q with P = omega w (A + 9/2 s^2),
+// Q = 3 omega w s, s = e_2k . u.  kCW and kCP are the float weights' exact
+// offsets: sum_i w_i - 1 = 2^-26 and sum_i e_ix^2 w_i - (float)(1/3) = -2^-27.
+constexpr float kCW = 0x1p-26f;
+constexpr float kCP = -0x1p-27f;
+
+// rho - 1, j and the second moments sum_i e_ia e_ib g_i (xx, yy, zz, xy, xz,
+// yz) from the nine opposite-pair sums and differences.
+template <typename M>
+__device__ __forceinline__ void dev_moments(const M g[19], M &dl, M &jx, M &jy, M &jz, M m2[6]) {
+    M s[9], t[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        s[k] = g[2 * k] + g[2 * k + 1];
+        t[k] = g[2 * k] - g[2 * k + 1];
+    }
+    const M a23 = s[2] + s[3], a45 = s[4] + s[5], a67 = s[6] + s[7];
+    dl = ((((s[0] + s[1]) + a23) + (a45 + a67)) + (s[8] + g[18])) + Bc<M>::of(kCW);
+    jx = ((t[0] + t[2]) + (t[3] + t[4])) + t[5];
+    jy = ((t[1] + t[2]) - t[3]) + (t[6] + t[7]);
+    jz = ((t[4] - t[5]) + (t[6] - t[7])) + t[8];
+    m2[0] = (s[0] + a23) + a45;
+    m2[1] = (s[1] + a23) + a67;
+    m2[2] = (s[8] + a45) + a67;
+    m2[3] = s[2] - s[3];
+    m2[4] = s[4] - s[5];
+    m2[5] = s[6] - s[7];
+}
+
+// One opposite pair: g_2k' = (1-omega) g_2k + P + Q, g_2k+1' = ... + P - Q.
+template <typename M>
+__device__ __forceinline__ void dev_pair(M g[19], int k, M v, M a, M b, M A, M om1) {
+    const M h = mfma(Bc<M>::of(K<float>::k45) * v, v, A);
+    const M P = a * h, Q = b * v;
+    g[2 * k] = mfma(om1, g[2 * k], P + Q);
+    g[2 * k + 1] = mfma(om1, g[2 * k + 1], P - Q);
+}
+
+// Relaxation of all 19 deviations with rate om towards the equilibrium of
+// (A, u).
+template <typename M>
+__device__ __forceinline__ void dev_relax(M g[19], M om, M A, M vx, M vy, M vz) {
+    const M om1 = Bc<M>::of(1.0f) - om;
+    const M a18 = om * Bc<M>::of(K<float>::c18), a36 = om * Bc<M>::of(K<float>::c36);
+    const M a3 = om * Bc<M>::of(K<float>::c3);
+    const M b18 = Bc<M>::of(K<float>::k3) * a18, b36 = Bc<M>::of(K<float>::k3) * a36;
+    dev_pair(g, 0, vx, a18, b18, A, om1);
+    dev_pair(g, 1, vy, a18, b18, A, om1);
+    dev_pair(g, 2, vx + vy, a36, b36, A, om1);
+    dev_pair(g, 3, vx - vy, a36, b36, A, om1);
+    dev_pair(g, 4, vx + vz, a36, b36, A, om1);
+    dev_pair(g, 5, vx - vz, a36, b36, A, om1);
+    dev_pair(g, 6, vy + vz, a36, b36, A, om1);
+    dev_pair(g, 7, vy - vz, a36, b36, A, om1);
+    dev_pair(g, 8, vz, a18, b18, A, om1);
+    g[18] = mfma(om1, g[18], a3 * A);
+}
+
+// Equilibrium deviations w_i (A + 3 e_i.u + 9/2 (e_i.u)^2) (lid cells).
+template <typename M>
+__device__ __forceinline__ void dev_equilibria(M vx, M vy, M vz, M A, M g[19]) {
+    const M w18 = Bc<M>::of(K<float>::c18), w36 = Bc<M>::of(K<float>::c36);
+    const M b18 = Bc<M>::of(K<float>::k3) * w18, b36 = Bc<M>::of(K<float>::k3) * w36;
+    const M v[9] = {vx, vy, vx + vy, vx - vy, vx + vz, vx - vz, vy + vz, vy - vz, vz};
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const bool axis = k < 2 || k == 8;
+        const M h = mfma(Bc<M>::of(K<float>::k45) * v[k], v[k], A);
+        const M P = (axis ? w18 : w36) * h, Q = (axis ? b18 : b36) * v[k];
+        g[2 * k] = P + Q;
+        g[2 * k + 1] = P - Q;
+    }
+    g[18] = Bc<M>::of(K<float>::c3) * A;
+}
+
+// Fluid collision in deviation form; with LES the Hou et al. rate from
+// Pi_ab = sum e_a e_b g + kCP delta_ab - (rho - 1)/3 delta_ab - u_a u_b,
+// omega = 2 / (tau0 + sqrt(tau0^2 + C sqrt(Pi:Pi))).
+template <typename M, bool LES>
+__device__ __forceinline__ void dev_collide(M g[19], M dl, M vx, M vy, M vz, const M m2[6], M A,
+                                            const LatDesc &d) {
+    M om = parm<M>(d, P_INV_TAU);
+    if (LES && par<float>(d, P_LES) != 0.0f) {
+        const M mc3 = Bc<M>::of(-K<float>::c3), cp = Bc<M>::of(kCP);
+        const M pxx = mfma(-vx, vx, mfma(mc3, dl, m2[0] + cp));
+        const M pyy = mfma(-vy, vy, mfma(mc3, dl, m2[1] + cp));
+        const M pzz = mfma(-vz, vz, mfma(mc3, dl, m2[2] + cp));
+        const M pxy = mfma(-vx, vy, m2[3]);
+        const M pxz = mfma(-vx, vz, m2[4]);
+        const M pyz = mfma(-vy, vz, m2[5]);
+        const M off = mfma(pyz, pyz, mfma(pxz, pxz, pxy * pxy));
+        const M dia = mfma(pzz, pzz, mfma(pyy, pyy, pxx * pxx));
+        const M q = mfma(Bc<M>::of(2.0f), off, dia);
+        const M tau0 = parm<M>(d, P_TAU0);
+        om = mdiv(Bc<M>::of(2.0f), tau0 + msqrt(mfma(parm<M>(d, P_LES), msqrt(q), tau0 * tau0)));
+    }
+    dev_relax(g, om, A, vx, vy, vz);
+}
+
+template <typename M>
+__device__ __forceinline__ M dev_dp1(M vx, M vy, M vz, M dl) {
+    const M u2 = mfma(vz, vz, mfma(vy, vy, vx * vx));
+    return mfma(Bc<M>::of(-K<float>::k15), u2, dl);
+}
+
+// The beta kernel's flag switch (as beta_case) in deviation form.  r is the
+// stored density: dd_param for fluid cells (lbm_beta.cl:493), the population
+// sum otherwise.
+template <typename M, bool LES>
+__device__ __forceinline__ void dev_beta(int fl, M g[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    M dl, m2[6];
+    dev_moments<M>(g, dl, vx, vy, vz, m2);
+    r = Bc<M>::of(1.0f) + dl;
+    if (fl == kFluid) {
+        const M A = dev_dp1(vx, vy, vz, dl);
+        dev_collide<M, LES>(g, dl, vx, vy, vz, m2, A, d);
+        r = Bc<M>::of(1.0f) + A;
+    } else if (fl == kObstacle) {
+        vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const M t = g[2 * k + 1];
+            g[2 * k + 1] = g[2 * k];
+            g[2 * k] = t;
+        }
+    } else if (fl == kLid) {
+        vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        const M A = Bc<M>::of(-K<float>::k15) * (vx * vx);
+        dev_equilibria<M>(vx, vy, vz, A, g);
+        r = Bc<M>::of(1.0f) + A;
+    }
+}
+
+// The alpha kernel's flag switch (as alpha_case) in deviation form.
+template <typename M, bool LES>
+__device__ __forceinline__ bool dev_alpha(int fl, M g[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    M dl, m2[6], t[9];
+    dev_moments<M>(g, dl, vx, vy, vz, m2);
+    r = Bc<M>::of(1.0f) + dl;
+    if (fl == kFluid) {
+        const M A = dev_dp1(vx, vy, vz, dl);
+        dev_collide<M, LES>(g, dl, vx, vy, vz, m2, A, d);
+        r = gravity_chain<M>(r, d, t);
+    } else if (fl == kLid) {
+        vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        const M A = Bc<M>::of(-K<float>::k15) * (vx * vx);
+        dev_equilibria<M>(vx, vy, vz, A, g);
+        r = gravity_chain<M>(Bc<M>::of(1.0f), d, t);
+    } else {
+        if (fl == kObstacle) {
+            vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
+        }
+        return false;
+    }
+    if (d.grav) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            g[2 * k + 1] -= t[k];
+            g[2 * k] += t[k];
+        }
+    }
+    return true;
+}
+
+// Moments plus flag switch for either form.
+template <typename M, bool LES, bool DEV>
+__device__ __forceinline__ void beta_phys(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    if constexpr (DEV) {
+        dev_beta<M, LES>(fl, f, r, vx, vy, vz, d);
+    } else {
+        moments_beta<M>(f, r, vx, vy, vz);
+        beta_case<M, LES>(fl, f, r, vx, vy, vz, d);
+    }
+}
+template <typename M, bool LES, bool DEV>
+__device__ __forceinline__ bool alpha_phys(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+    if constexpr (DEV) {
+        return dev_alpha<M, LES>(fl, f, r, vx, vy, vz, d);
+    } else {
+        moments_alpha<M>(f, r, vx, vy, vz);
+        return alpha_case<M, LES>(fl, f, r, vx, vy, vz, d);
+    }
+}
+
 __device__ __forceinline__ int64_t dir_off(int i, int64_t nx, int64_t slice) {
     return (int64_t)dir_x(i) + (int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * slice;
 }
@@ -447,16 +690,15 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
     for (int i = 0; i < 19; i++) {
         const int64_t off = dir_off(i, nx, sl);
         const S *p = WRAP ? dd + opp(i) * ps + wrap_cell(c, -off, n) : pc + (opp(i) * ps - off);
-        f[i] = Store<S>::ld(p, weight<R>(i));
+        f[i] = pop_ld<S>(p, i);
     }
     R r, vx, vy, vz;
-    moments_beta<R>(f, r, vx, vy, vz);
-    beta_case<R, LES>(fl, f, r, vx, vy, vz, d);
+    beta_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d);
 #pragma unroll
     for (int i = 0; i < 19; i++) {
         const int64_t off = dir_off(i, nx, sl);
         S *p = WRAP ? dd + i * ps + wrap_cell(c, off, n) : pc + (i * ps + off);
-        Store<S>::st(p, f[i], weight<R>(i));
+        pop_st<S>(p, f[i], i);
     }
     if (fl == kGhost) return;  // lbm_beta.cl:787-788
     if (store_v) {
@@ -466,9 +708,9 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_beta(const __grid_constant__ StepArgs a) {
-    const LatDesc &d = lattice_of<PT>(a);
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_beta(const __grid_constant__ DomainArgs a) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
     if (c >= d.n) return;
@@ -488,13 +730,12 @@ __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int stor
     const int64_t ps = d.pstride;
     R f[19];
 #pragma unroll
-    for (int i = 0; i < 19; i++) f[i] = Store<S>::ld(pc + i * ps, weight<R>(i));
+    for (int i = 0; i < 19; i++) f[i] = pop_ld<S>(pc + i * ps, i);
     R r, vx, vy, vz;
-    moments_alpha<R>(f, r, vx, vy, vz);
-    if (alpha_case<R, LES>(fl, f, r, vx, vy, vz, d)) {
+    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d)) {
         // each population goes to the opposite slot (lbm_alpha.cl:185-301)
 #pragma unroll
-        for (int i = 0; i < 19; i++) Store<S>::st(pc + opp(i) * ps, f[i], weight<R>(i));
+        for (int i = 0; i < 19; i++) pop_st<S>(pc + opp(i) * ps, f[i], opp(i));
     }
     if (store_v) {
         R *u = (R *)d.vel + c;
@@ -503,9 +744,9 @@ __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int stor
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ StepArgs a) {
-    const LatDesc &d = lattice_of<PT>(a);
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ DomainArgs a) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
@@ -559,33 +800,32 @@ __device__ __forceinline__ void beta_pair(const LatDesc &d, int64_t c, int lane,
 #pragma unroll
     for (int i = 0; i < 19; i++) {
         const int ex = dir_x(i);
-        const R w = weight<R>(i);
         // aligned pair (c, c+1) of the source row: c - e_i without its x part
         const S *p = dd + opp(i) * ps + c - ((int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * sl);
-        const P2 q = Store<S>::ld2(p, w);
+        const P2 q = pop_ld2<S>(p, i);
         if (ex == 0) {
             f[i] = q;
         } else if (ex > 0) {  // sources (c-1, c)
             float lo = __shfl_up_sync(kFull, q.y, 1);
-            if (lane == 0) lo = Store<S>::ld(p - 1, w);
+            if (lane == 0) lo = pop_ld<S>(p - 1, i);
             f[i] = P2{lo, q.x};
         } else {  // sources (c+1, c+2)
             float hi = __shfl_down_sync(kFull, q.x, 1);
-            if (lane == 31) hi = Store<S>::ld(p + 2, w);
+            if (lane == 31) hi = pop_ld<S>(p + 2, i);
             f[i] = P2{q.y, hi};
         }
     }
+    constexpr bool DEV = Store<S>::kDev;
     P2 r, vx, vy, vz;
-    moments_beta<P2>(f, r, vx, vy, vz);
     if (fl0 == kFluid && fl1 == kFluid) {
-        beta_case<P2, LES>(kFluid, f, r, vx, vy, vz, d);
+        beta_phys<P2, LES, DEV>(kFluid, f, r, vx, vy, vz, d);
     } else {
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            R g[19], rr = h ? r.y : r.x, ux = h ? vx.y : vx.x, uy = h ? vy.y : vy.x, uz = h ? vz.y : vz.x;
+            R g[19], rr, ux, uy, uz;
 #pragma unroll
             for (int i = 0; i < 19; i++) g[i] = h ? f[i].y : f[i].x;
-            beta_case<R, LES>(h ? fl1 : fl0, g, rr, ux, uy, uz, d);
+            beta_phys<R, LES, DEV>(h ? fl1 : fl0, g, rr, ux, uy, uz, d);
 #pragma unroll
             for (int i = 0; i < 19; i++) (h ? f[i].y : f[i].x) = g[i];
             (h ? r.y : r.x) = rr; (h ? vx.y : vx.x) = ux; (h ? vy.y : vy.x) = uy; (h ? vz.y : vz.x) = uz;
@@ -594,28 +834,27 @@ __device__ __forceinline__ void beta_pair(const LatDesc &d, int64_t c, int lane,
 #pragma unroll
     for (int i = 0; i < 19; i++) {
         const int ex = dir_x(i);
-        const R w = weight<R>(i);
         S *p = dd + i * ps + c + ((int64_t)dir_y(i) * nx + (int64_t)dir_z(i) * sl);
         if (ex == 0) {
-            Store<S>::st2(p, f[i], w);
+            pop_st2<S>(p, f[i], i);
         } else if (ex > 0) {  // destinations (c+1, c+2)
             const float lo = __shfl_up_sync(kFull, f[i].y, 1);
-            if (lane != 0) Store<S>::st2(p, P2{lo, f[i].x}, w);
-            else Store<S>::st(p + 1, f[i].x, w);
-            if (lane == 31) Store<S>::st(p + 2, f[i].y, w);
+            if (lane != 0) pop_st2<S>(p, P2{lo, f[i].x}, i);
+            else pop_st<S>(p + 1, f[i].x, i);
+            if (lane == 31) pop_st<S>(p + 2, f[i].y, i);
         } else {  // destinations (c-1, c)
             const float hi = __shfl_down_sync(kFull, f[i].x, 1);
-            if (lane != 31) Store<S>::st2(p, P2{f[i].y, hi}, w);
-            else Store<S>::st(p, f[i].y, w);
-            if (lane == 0) Store<S>::st(p - 1, f[i].x, w);
+            if (lane != 31) pop_st2<S>(p, P2{f[i].y, hi}, i);
+            else pop_st<S>(p, f[i].y, i);
+            if (lane == 0) pop_st<S>(p - 1, f[i].x, i);
         }
     }
     store_pair_moments(d, c, fl0, fl1, r, vx, vy, vz, store_v, store_rho);
 }
 
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, 2) k_beta2(const __grid_constant__ StepArgs a) {
-    const LatDesc &d = lattice_of<PT>(a);
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, 2) k_beta2(const __grid_constant__ DomainArgs a) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * kPairCells;
     const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny + 2;
     if (c0 < reach || c0 + kPairCells + reach >= d.n) {
@@ -639,24 +878,25 @@ __device__ __forceinline__ void alpha_pair(const LatDesc &d, int64_t c, int stor
     if (fl0 == kGhost && fl1 == kGhost) return;  // lbm_alpha.cl:31-32
     P2 f[19];
 #pragma unroll
-    for (int i = 0; i < 19; i++) f[i] = Store<S>::ld2(pc + i * ps, weight<R>(i));
+    for (int i = 0; i < 19; i++) f[i] = pop_ld2<S>(pc + i * ps, i);
+    constexpr bool DEV = Store<S>::kDev;
     P2 r, vx, vy, vz;
-    moments_alpha<P2>(f, r, vx, vy, vz);
     if (fl0 == kFluid && fl1 == kFluid) {
-        alpha_case<P2, LES>(kFluid, f, r, vx, vy, vz, d);
+        alpha_phys<P2, LES, DEV>(kFluid, f, r, vx, vy, vz, d);
 #pragma unroll
-        for (int i = 0; i < 19; i++) Store<S>::st2(pc + opp(i) * ps, f[i], weight<R>(i));
+        for (int i = 0; i < 19; i++) pop_st2<S>(pc + opp(i) * ps, f[i], opp(i));
     } else {
+        r = vx = vy = vz = P2{0.0f, 0.0f};
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int fl = h ? fl1 : fl0;
             if (fl == kGhost) continue;
-            R g[19], rr = h ? r.y : r.x, ux = h ? vx.y : vx.x, uy = h ? vy.y : vy.x, uz = h ? vz.y : vz.x;
+            R g[19], rr, ux, uy, uz;
 #pragma unroll
             for (int i = 0; i < 19; i++) g[i] = h ? f[i].y : f[i].x;
-            if (alpha_case<R, LES>(fl, g, rr, ux, uy, uz, d)) {
+            if (alpha_phys<R, LES, DEV>(fl, g, rr, ux, uy, uz, d)) {
 #pragma unroll
-                for (int i = 0; i < 19; i++) Store<S>::st(pc + opp(i) * ps + h, g[i], weight<R>(i));
+                for (int i = 0; i < 19; i++) pop_st<S>(pc + opp(i) * ps + h, g[i], opp(i));
             }
             (h ? r.y : r.x) = rr; (h ? vx.y : vx.x) = ux; (h ? vy.y : vy.x) = uy; (h ? vz.y : vz.x) = uz;
         }
@@ -664,9 +904,9 @@ __device__ __forceinline__ void alpha_pair(const LatDesc &d, int64_t c, int stor
     store_pair_moments(d, c, fl0, fl1, r, vx, vy, vz, store_v, store_rho);
 }
 
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ StepArgs a) {
-    const LatDesc &d = lattice_of<PT>(a);
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ DomainArgs a) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c = (int64_t)(blockIdx.x - d.first_block) * kPairCells + 2 * threadIdx.x;
     if (c + 1 < d.n) alpha_pair<S, LES>(d, c, a.store_v, a.store_rho);
     else if (c < d.n) alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
@@ -677,9 +917,11 @@ __global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ StepA
 // a beta step for a lattice whose counter was even at the tick start and j
 // even (and so on), chosen per block.  Used for ensembles of cavities and
 // for the serving loop, where solves start at different times.
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_step(const __grid_constant__ StepArgs a, int j) {
-    const LatDesc &d = lattice_of<PT>(a);
+// k_step holds both kernels' code: without the subgrid model it takes the
+// alpha kernel's register budget.
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, LES>())) k_step(const __grid_constant__ BatchArgs a, int j) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
     if (c >= d.n) return;
@@ -694,9 +936,9 @@ __global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_step(cons
         beta_cell<S, LES, false>(d, c, a.store_v, a.store_rho);
 }
 
-template <typename S, bool LES, bool PT>
-__global__ void __launch_bounds__(256, 2) k_step2(const __grid_constant__ StepArgs a, int j) {
-    const LatDesc &d = lattice_of<PT>(a);
+template <typename S, bool LES>
+__global__ void __launch_bounds__(256, 2) k_step2(const __grid_constant__ BatchArgs a, int j) {
+    const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * kPairCells;
     if ((d.parity + j) & 1) {
         const int64_t c = c0 + 2 * threadIdx.x;
