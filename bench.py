@@ -235,7 +235,7 @@ def make_params(api, storage):
     return api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
 
 
-def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None):
+def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None):
     """K timed steps of one domain with a CUDA-event pair around every step
     kernel; returns (wall ms of the K steps, step-kernel ms per launch,
     graph-replay MLUPS, cells)."""
@@ -244,6 +244,8 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None):
     D = api.Domain(size, nums, api.STORAGE_NAMES[storage], store_velocity=False, store_density=False)
     D.set_params(make_params(api, storage))
     D.set_halo_mode(HALO_MODE)
+    if shape:
+        D.set_kernel_shape(shape)
     D.reset()
     D.perturb(SEED, AMP)
     D.run(warmup, use_graph=False)
@@ -295,7 +297,8 @@ def run_gpu(args):
         dist.barrier()
 
     with ClockSampler(local) as clk:
-        ms, k_ms, graph_mlups, cells = measure(api, args.size, args.nums, "f32", args.steps, args.warmup, dist)
+        ms, k_ms, graph_mlups, cells = measure(api, args.size, args.nums, args.storage, args.steps, args.warmup, dist,
+                                               shape=args.shape)
     ms = max_over_ranks(ms, dist)
     mlups = whole_job_mlups(cells, args.steps, ms, ws)
     if args.steps < 2:
@@ -303,9 +306,9 @@ def run_gpu(args):
 
     # roofline of the step kernel
     peak, peak_kind = measured_peak()
-    alg_bytes = BYTES_PER_CELL["f32"] * cells
+    alg_bytes = BYTES_PER_CELL[args.storage] * cells
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    traffic = profiled_traffic()
+    traffic = profiled_traffic() if args.storage == "f32" else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": round(traffic * cells) if traffic else None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
@@ -347,8 +350,9 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config_dict(None if tuple(args.size) == SIZE else f"profiling size {args.size}"),
+        "scaling": "weak", "vs_baseline": None, "dtype": args.storage, "data": "synthetic",
+        "config": config_dict(None if tuple(args.size) == SIZE and args.storage == "f32"
+                              else f"profiling size {args.size}, storage {args.storage}"),
         "roofline": roofline, "e2e": e2e,
         "gpu_launches": int(args.steps * (1 + 2)),
         "clocks": clk.summary(),
@@ -373,6 +377,8 @@ def run_e2e(api, prm, steps):
     D = api.Domain(SIZE, NUMS, api.F32, store_velocity=True, store_density=False)
     D.set_params(prm)
     D.set_halo_mode(HALO_MODE)
+    if shape:
+        D.set_kernel_shape(shape)
     D.reset()
     D.perturb(SEED, AMP)
     D.set_store_interval(0)  # velocity written on the last step only
@@ -420,6 +426,10 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the extra storage / size measurements")
     ap.add_argument("--size", type=int, nargs=3, default=list(SIZE), help="domain size (profiling only)")
     ap.add_argument("--nums", type=int, nargs=3, default=list(NUMS), help="subdomains (profiling only)")
+    ap.add_argument("--storage", default="f32", choices=["f32", "f64", "f16", "bf16"],
+                    help="population storage of the main measurement (profiling only)")
+    ap.add_argument("--shape", type=int, default=None, choices=[1, 2, 3],
+                    help="step kernel shape of the main measurement (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -70,11 +70,13 @@ def test_init_matches_oracle(capi, oracle_mod, storage):
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
 @pytest.mark.parametrize("cs", [0.0, 0.17])
 @pytest.mark.parametrize("gravity", [(0.0, 0.0, 0.0), (1e-5, -2e-5, 3e-6)])
-@pytest.mark.parametrize("dims,shape", [((21, 14, 11), 1), ((22, 14, 11), 2), ((64, 12, 18), 2)])
+@pytest.mark.parametrize("dims,shape", [((21, 14, 11), 1), ((22, 14, 11), 2), ((64, 12, 18), 2),
+                                        ((21, 14, 11), 3), ((64, 12, 18), 3)])
 def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity, dims, shape):
-    """Perturbed lid cavity: every array, every step, for the one-cell and
-    the two-cell kernel shapes (the latter needs an even x extent; the 64-wide
-    case has whole warps inside the lattice)."""
+    """Perturbed lid cavity: every array, every step, for the one-cell, the
+    two-cell (needs an even x extent; the 64-wide case has whole warps inside
+    the lattice) and the staged-tile kernel shapes (the 64x12x18 case spans
+    many tiles and ends in a partial one)."""
     api, O = capi, oracle_mod
     p = oracle_params(O, storage, dims, cs, gravity)
     L = gpu_single(api, O, dims, storage, p, perturb=(SEED, 2e-2))
@@ -108,7 +110,7 @@ def test_matches_reference_arrays(capi, oracle_mod, storage):
             assert n_diff(rho, g[f"rho{k}"]) == 0, f"step {k}"
 
 
-@pytest.mark.parametrize("storage,shape", [("f32", 1), ("f32", 2), ("f64", 1)])
+@pytest.mark.parametrize("storage,shape", [("f32", 1), ("f32", 2), ("f32", 3), ("f64", 1)])
 def test_c1_matches_reference_every_step(capi, oracle_mod, storage, shape):
     """Config 1 geometry (64^3 lid cavity, Re 1000, U 0.05, rest start) with
     the reference's plain BGK: the state hash equals the reference kernels'
@@ -147,7 +149,7 @@ def test_c1_smagorinsky_matches_oracle(capi, oracle_mod):
         compare(api, O, L, s, "f32", f"after step {k + 1}")
 
 
-@pytest.mark.parametrize("use_graph,shape", [(False, 1), (True, 1), (True, 2)])
+@pytest.mark.parametrize("use_graph,shape", [(False, 1), (True, 1), (True, 2), (True, 3), (False, 3)])
 def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph, shape):
     """2x2x1 decomposition on one GPU: every subdomain's state hash equals the
     reference kernels' with the reference host exchange, every step."""

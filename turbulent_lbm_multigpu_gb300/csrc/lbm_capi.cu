@@ -420,6 +420,12 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab) {
     return true;
 }
 
+int effective_shape(int storage, int shape, const LatDesc *tab, int ntab) {
+    if (shape == 2 && pair_shape(storage, tab, ntab)) return 2;
+    if (shape == 3 && storage != kF64) return 3;
+    return 1;
+}
+
 static int launch_chunk(int storage, bool pair, int parity, bool les, const DomainArgs &a, int blocks,
                         cudaStream_t st) {
     if (pair) {
@@ -439,23 +445,83 @@ static int launch_chunk(int storage, bool pair, int parity, bool les, const Doma
     return fail("unknown storage type");
 }
 
-// One step over `ntab` lattices of one storage type, kParamLattices per
-// launch.  `htab` holds the descriptors with nblocks for the launch shape.
-int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
+// Streaming multiprocessors of the current device (cached per device).
+static int sm_count() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!cache[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = v > 0 ? v : 1;
+    }
+    return cache[dev];
+}
+
+template <typename S, bool LES, bool BETA>
+static int launch_staged_k(const DomainArgs &a, int tiles, cudaStream_t st) {
+    static bool attr = false;  // the ring exceeds the default 48 KB of dynamic shared memory
+    if (!attr) {
+        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                Tile<S>::SMEM));
+        attr = true;
+    }
+    const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
+    k_step_staged<S, LES, BETA><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
+    CU(cudaGetLastError());
+    return 0;
+}
+
+template <typename S>
+static int launch_staged_t(int parity, bool les, const DomainArgs &a, int tiles, cudaStream_t st) {
+    if (tiles <= 0) return 0;
+    if (parity) return les ? launch_staged_k<S, true, false>(a, tiles, st) : launch_staged_k<S, false, false>(a, tiles, st);
+    return les ? launch_staged_k<S, true, true>(a, tiles, st) : launch_staged_k<S, false, true>(a, tiles, st);
+}
+
+static int staged_cells(int storage) {
+    switch (storage) {
+        case kF32: return Tile<float>::T;
+        case kF16: return Tile<__half>::T;
+        case kBF16: return Tile<__nv_bfloat16>::T;
+    }
+    return 0;
+}
+
+int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
                 cudaStream_t st) {
+    // the staged beta needs rows of whole 128-byte lines (nx a multiple of 32
+    // float or 64 half populations)
+    bool staged = shape == 3 && storage != kF64;
+    if (staged && parity == 0)
+        for (int i = 0; i < ntab; i++)
+            if ((htab[i].nx * storage_bytes(storage)) % 128) staged = false;
+    const bool pair = shape == 2;
+    const int per = staged ? staged_cells(storage) : cells_per_block(pair);
     for (int c0 = 0; c0 < ntab; c0 += kParamLattices) {
         DomainArgs a;
         memset(&a, 0, sizeof(a));
         a.ntab = std::min(kParamLattices, ntab - c0);
         a.store_v = sv;
         a.store_rho = sr;
-        int blocks = 0;
+        int units = 0;
         for (int i = 0; i < a.ntab; i++) {
             a.tab[i] = htab[c0 + i];
-            a.tab[i].first_block = blocks;
-            blocks += a.tab[i].nblocks;
+            a.tab[i].first_block = units;
+            a.tab[i].nblocks = (int)((a.tab[i].n + per - 1) / per);
+            units += a.tab[i].nblocks;
         }
-        if (launch_chunk(storage, pair, parity, les, a, blocks, st)) return -1;
+        int rc;
+        if (staged) {
+            switch (storage) {
+                case kF32: rc = launch_staged_t<float>(parity, les, a, units, st); break;
+                case kF16: rc = launch_staged_t<__half>(parity, les, a, units, st); break;
+                default: rc = launch_staged_t<__nv_bfloat16>(parity, les, a, units, st); break;
+            }
+        } else {
+            rc = launch_chunk(storage, pair, parity, les, a, units, st);
+        }
+        if (rc) return -1;
     }
     return 0;
 }
@@ -518,6 +584,13 @@ const char *lbm_cu_version(void) {
 int lbm_cu_synchronize(void *stream) {
     if (stream) CU(cudaStreamSynchronize(S(stream)));
     else CU(cudaDeviceSynchronize());
+    unsigned int err = 0;
+    CU(cudaMemcpyFromSymbol(&err, g_stage_error, sizeof(err)));
+    if (err) {
+        const unsigned int zero = 0;
+        CU(cudaMemcpyToSymbol(g_stage_error, &zero, sizeof(zero)));
+        return fail("a staged step kernel gave up waiting for its bulk copies");
+    }
     return 0;
 }
 
@@ -621,11 +694,9 @@ int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t see
 
 int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
     if (!l) return fail("NULL lattice");
-    LatDesc h = l->h;
-    const bool pair = l->allow_pair && pair_shape(l->storage, &h, 1);
-    h.first_block = 0;
-    h.nblocks = (int)((l->n + cells_per_block(pair) - 1) / cells_per_block(pair));
-    return launch_step(l->storage, pair, parity & 1, uses_les(h), &h, 1, l->store_v, l->store_rho, S(stream));
+    const LatDesc &h = l->h;
+    return launch_step(l->storage, effective_shape(l->storage, l->shape, &h, 1), parity & 1, uses_les(h), &h, 1,
+                       l->store_v, l->store_rho, S(stream));
 }
 
 static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], void *host, const int norm[3],
@@ -868,8 +939,9 @@ struct lbm_domain {
     std::vector<std::vector<CommGeom>> comms;
     std::vector<std::vector<int>> bc;
     std::vector<int> coords;  // 3 per subdomain
-    std::vector<LatDesc> h_tab[2];  // [one-cell, two-cell] block counts
-    bool pair = false;
+    std::vector<LatDesc> h_tab;  // descriptors of the subdomains
+    int shape = 1;               // requested kernel shape
+    int eff_shape = 1;           // the shape the subdomains run
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
     std::vector<HaloDesc> plan[2][3];
@@ -877,7 +949,6 @@ struct lbm_domain {
     int64_t plan_cells[2][3] = {};
     int plan_planes[2][3] = {};
     int halo_mode = 0;  // 0: all 19 populations after alpha (reference), 1: the 5 read inward
-    bool allow_pair = false;
     int64_t counter = 0;
     int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
     cudaGraphExec_t graph = nullptr;
@@ -945,17 +1016,9 @@ int domain_build_plans(lbm_domain *D) {
 int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
     (void)st;
     if (!D->tab_dirty) return 0;
-    for (int shape = 0; shape < 2; shape++) {
-        std::vector<LatDesc> tab;
-        const int per = cells_per_block(shape == 1);
-        for (auto *l : D->subs) {
-            LatDesc h = l->h;
-            h.nblocks = (int)((l->n + per - 1) / per);
-            tab.push_back(h);
-        }
-        D->h_tab[shape] = tab;
-    }
-    D->pair = D->allow_pair && pair_shape(D->storage, D->h_tab[1].data(), (int)D->subs.size());
+    D->h_tab.clear();
+    for (auto *l : D->subs) D->h_tab.push_back(l->h);
+    D->eff_shape = effective_shape(D->storage, D->shape, D->h_tab.data(), (int)D->h_tab.size());
     D->tab_dirty = false;
     return 0;
 }
@@ -976,8 +1039,7 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
     const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (timed && domain_record(D, st, &e0)) return -1;
-    const int sh = D->pair ? 1 : 0;
-    if (launch_step(D->storage, D->pair, parity, les, D->h_tab[sh].data(), (int)D->subs.size(), sv, sr, st))
+    if (launch_step(D->storage, D->eff_shape, parity, les, D->h_tab.data(), (int)D->subs.size(), sv, sr, st))
         return -1;
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
@@ -1172,15 +1234,15 @@ int lbm_cu_domain_set_store_interval(lbm_domain *D, int interval) {
 
 int lbm_cu_set_kernel_shape(lbm_lattice *l, int cells_per_thread) {
     if (!l) return fail("NULL lattice");
-    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
-    l->allow_pair = cells_per_thread == 2;
+    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("kernel shape is 1, 2 or 3");
+    l->shape = cells_per_thread;
     return 0;
 }
 
 int lbm_cu_domain_set_kernel_shape(lbm_domain *D, int cells_per_thread) {
     if (!D) return fail("NULL domain");
-    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
-    D->allow_pair = cells_per_thread == 2;
+    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("kernel shape is 1, 2 or 3");
+    D->shape = cells_per_thread;
     D->tab_dirty = true;
     drop_graph(D);
     return 0;

@@ -39,10 +39,15 @@ inline bool uses_les(const LatDesc &h) { return h.pd[P_LES] != 0.0; }
 bool pair_shape(int storage, const LatDesc *tab, int ntab);
 inline int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
 
+// Kernel shapes of a step: 1 one cell per thread, 2 two cells per thread,
+// 3 tiles staged through shared memory by bulk copies.
+// The shape a set of lattices runs: 2 needs float arithmetic and even nx,
+// 3 float/half/bfloat16 storage; otherwise 1.
+int effective_shape(int storage, int shape, const LatDesc *tab, int ntab);
+
 // One step over `ntab` lattices of one storage type, kParamLattices
-// descriptors per launch; `htab` holds the descriptors with nblocks for the
-// launch shape.
-int launch_step(int storage, bool pair, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
+// descriptors per launch.
+int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
                 cudaStream_t st);
 }  // namespace lbm_rt
 
@@ -60,5 +65,5 @@ struct lbm_lattice {
     bool dirty = true;
     void *stage = nullptr;  // staging for host copies and reduction partials
     size_t stage_bytes = 0;
-    bool allow_pair = false;  // two-cell kernels where the shape allows (tuning option)
+    int shape = 1;  // requested kernel shape (tuning option, see effective_shape)
 };

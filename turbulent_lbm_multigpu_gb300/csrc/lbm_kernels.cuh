@@ -242,6 +242,7 @@ template <int N> struct StepArgs {
 };
 using DomainArgs = StepArgs<kParamLattices>;
 using BatchArgs = StepArgs<kBatchLattices>;
+static_assert(sizeof(BatchArgs) + sizeof(int) <= 32764, "kernel parameters exceed 32 KB");
 
 // Lattice of this block: one load from the block map, else a binary search
 // on first_block.
@@ -666,11 +667,12 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
 }
 
 // Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
-// registers) where the one-cell float kernels fit without spilling, fewer
+// registers) for the one-cell float kernels with the subgrid model, 3 (80)
+// without it (its straight-line code schedules with more live values), 1
 // for double.
-template <typename S, bool LES, bool BETA>
+template <typename S, bool LES>
 __host__ __device__ constexpr int min_blocks() {
-    return sizeof(typename Store<S>::R) == 8 ? 1 : LES ? 4 : (BETA && sizeof(S) == 4) ? 4 : 3;
+    return sizeof(typename Store<S>::R) == 8 ? 1 : LES ? 4 : 3;
 }
 
 // ---------------------------------------------------- one cell per thread
@@ -709,7 +711,7 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
 }
 
 template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, true>())) k_beta(const __grid_constant__ DomainArgs a) {
+__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_beta(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
@@ -745,7 +747,7 @@ __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int stor
 }
 
 template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, false>())) k_alpha(const __grid_constant__ DomainArgs a) {
+__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_alpha(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
     const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
@@ -912,15 +914,291 @@ __global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ Domai
     else if (c < d.n) alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
 }
 
+// ------------------------------------------------ tiles staged by TMA
+// The staged kernels move tiles of T consecutive cells between HBM and
+// shared memory with the Tensor Memory Accelerator's bulk copies
+// (cp.async.bulk).  A persistent block has one producer warp and eight
+// compute warps around a ring of kStages tile buffers: the producer keeps
+// the next tiles' 19 plane segments (+ flag bytes) in flight while the
+// compute warps work on the current one from shared memory ("full" /
+// "empty" mbarriers per buffer, no block-wide barrier in the loop).  This
+// decouples the bytes in flight from the registers of the collision (the
+// one-cell kernels are latency-bound at 64 registers a thread) and removes
+// the per-population 64-bit address arithmetic of the loads.
+//   alpha: segment i is plane i of the tile itself; the updated populations
+//          go back into the segments (slot opp(i)) and the producer writes
+//          the tile back with bulk stores.
+//   beta:  segment i holds the tile's sources of f_i, plane opp(i) at
+//          c - e_i, from the 128-byte line below (T + A elements; nx is a
+//          multiple of A, so the offset into the segment is fixed per
+//          direction); the results scatter to c + e_i with ordinary
+//          stores.  Tiles within reach of either end of the buffer (their
+//          sources wrap) and a partial last tile take the one-cell path
+//          with the wrap instead.
+// Every wait on a barrier is bounded; a wait that runs out records
+// kStageTimeout in g_stage_error and the warp stops.
+constexpr int kStages = 3;
+constexpr int kStageBlocksPerSM = 3;
+constexpr int kConsumerWarps = 8;
+constexpr int kStageThreads = 32 * (kConsumerWarps + 1);
+constexpr unsigned kStageTimeout = 1u;
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+
+__device__ unsigned int g_stage_error;
+
+template <typename S> struct Tile {
+    static_assert(sizeof(S) <= 4, "staged tiles hold float, half or bfloat16 populations");
+    static constexpr int T = 1024 / (int)sizeof(S);  // cells per tile: 1 KB per plane
+    static constexpr int A = 128 / (int)sizeof(S);   // elements per 128-byte line
+    static constexpr int PER = T / (32 * kConsumerWarps);  // cells per compute thread
+    static constexpr int SEG = (T + A) * (int)sizeof(S);   // bytes per plane segment
+    static constexpr int STAGE = 19 * SEG + T;       // 19 segments + flag bytes
+    static constexpr int SMEM = 128 + kStages * STAGE;  // barriers + the ring
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kStageWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Lattice of tile t (first_block / nblocks count tiles here).
+template <int N>
+__device__ __forceinline__ const LatDesc &lattice_of_unit(const StepArgs<N> &a, int t) {
+    int li = 0, hi = a.ntab - 1;
+    while (li < hi) {
+        const int mid = (li + hi + 1) >> 1;
+        if (a.tab[mid].first_block <= t) li = mid; else hi = mid - 1;
+    }
+    return a.tab[li];
+}
+
+// A beta tile whose shifted segments lie inside the lattice: every source
+// range [c0 - off_i - (A - 1), c0 - off_i + T + A) within [0, n).
+template <typename S>
+__device__ __forceinline__ bool beta_tile_inside(const LatDesc &d, int64_t c0) {
+    using TL = Tile<S>;
+    const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny + 1;
+    return c0 >= reach + TL::A && c0 + TL::T + TL::A + reach <= d.n;
+}
+
+// Issue the bulk loads of tile t into a ring buffer: lane i < 19 copies
+// plane segment i, lane 19 the flag bytes (the producer warp spreads the
+// address arithmetic over its lanes).  A beta tile that is not inside gets
+// no copies: its phase completes at once and the compute warps read it from
+// global memory.
+template <typename S, bool BETA>
+__device__ __forceinline__ void stage_tile(const DomainArgs &a, int t, unsigned char *stage, uint64_t *bar,
+                                           int lane) {
+    using TL = Tile<S>;
+    const LatDesc &d = lattice_of_unit(a, t);
+    const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
+    const bool inside = !BETA || beta_tile_inside<S>(d, c0);
+    const int cells = (int)min((int64_t)TL::T, d.n - c0);
+    const uint32_t pb = BETA ? (uint32_t)TL::SEG : (uint32_t)((cells * (int)sizeof(S) + 15) & ~15);
+    const uint32_t fb = BETA ? (uint32_t)TL::T : (uint32_t)((cells + 15) & ~15);
+    if (lane == 0) mbar_expect_tx(bar, inside ? 19 * pb + fb : 0);
+    __syncwarp();
+    if (!inside) return;
+    if (lane < 19) {
+        int64_t start = c0;
+        if (BETA) {
+            const int64_t off = (int64_t)dir_x(lane) + (int64_t)dir_y(lane) * d.nx + (int64_t)dir_z(lane) * d.nx * d.ny;
+            start = (c0 - off) & ~(int64_t)(TL::A - 1);
+        }
+        const int plane = BETA ? opp(lane) : lane;
+        bulk_load(stage + lane * TL::SEG, (const S *)d.dd + plane * d.pstride + start, pb, bar);
+    } else if (lane == 19) {
+        bulk_load(stage + 19 * TL::SEG, d.flags + c0, fb, bar);
+    }
+}
+
+// Write an alpha tile back from its ring buffer, lane i < 19 plane i, and
+// wait until the buffer has been read out.
+template <typename S>
+__device__ __forceinline__ void unstage_tile(const DomainArgs &a, int t, const unsigned char *stage, int lane) {
+    using TL = Tile<S>;
+    if (lane < 19) {
+        const LatDesc &d = lattice_of_unit(a, t);
+        const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
+        const int cells = (int)min((int64_t)TL::T, d.n - c0);
+        const uint32_t pb = (uint32_t)((cells * (int)sizeof(S) + 15) & ~15);
+        bulk_store((S *)d.dd + lane * d.pstride + c0, stage + lane * TL::SEG, pb);
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+    __syncwarp();
+}
+
+// One beta cell of an inside tile: sources from the ring buffer (the
+// offset (-e_i . (1, nx, nx ny)) mod A is -e_ix mod A because A divides
+// nx), results scattered to the neighbours.
+template <typename S, bool LES>
+__device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
+                                                 int store_v, int store_rho) {
+    using TL = Tile<S>;
+    using R = typename Store<S>::R;
+    const int64_t nx = d.nx, sl = (int64_t)d.nx * d.ny, ps = d.pstride;
+    const int fl = stage[19 * TL::SEG + l];
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) {
+        const int rem = (-dir_x(i)) & (TL::A - 1);
+        f[i] = pop_ld<S>((const S *)(stage + i * TL::SEG) + (l + rem), i);
+    }
+    R r, vx, vy, vz;
+    beta_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d);
+    S *const pc = (S *)d.dd + c;
+#pragma unroll
+    for (int i = 0; i < 19; i++) pop_st<S>(pc + (i * ps + dir_off(i, nx, sl)), f[i], i);
+    if (fl == kGhost) return;  // lbm_beta.cl:787-788
+    if (store_v) {
+        R *u = (R *)d.vel + c;
+        u[0] = vx; u[d.n] = vy; u[2 * d.n] = vz;
+    }
+    if (store_rho) ((R *)d.rho)[c] = r;
+}
+
+template <typename S, bool LES>
+__device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned char *stage, int l, int64_t c,
+                                                  int store_v, int store_rho) {
+    using TL = Tile<S>;
+    using R = typename Store<S>::R;
+    const int fl = stage[19 * TL::SEG + l];
+    if (fl == kGhost) return;  // lbm_alpha.cl:31-32
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; i++) f[i] = pop_ld<S>((const S *)(stage + i * TL::SEG) + l, i);
+    R r, vx, vy, vz;
+    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d)) {
+#pragma unroll
+        for (int i = 0; i < 19; i++) pop_st<S>((S *)(stage + opp(i) * TL::SEG) + l, f[i], opp(i));
+    }
+    if (store_v) {
+        R *u = (R *)d.vel + c;
+        u[0] = vx; u[d.n] = vy; u[2 * d.n] = vz;
+    }
+    if (store_rho) ((R *)d.rho)[c] = r;
+}
+
+template <typename S, bool LES, bool BETA>
+__global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ DomainArgs a,
+                                                                                  int tiles) {
+    using TL = Tile<S>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *full = (uint64_t *)smem, *empty = full + kStages;
+    unsigned char *buf = smem + 128;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumerWarps);
+        }
+        fence_barrier_init();
+    }
+    __syncthreads();
+    const int stride = gridDim.x;
+    const int mine = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / stride + 1 : 0;
+
+    if (warp == kConsumerWarps) {  // producer warp
+        bool ok = true;
+        const int rounds = mine + (BETA ? 0 : kStages);
+        for (int k = 0; k < rounds; ++k) {
+            const int s = k % kStages;
+            unsigned char *stage = buf + s * TL::STAGE;
+            if (k >= kStages) {
+                // the compute warps are done with the tile k - kStages in this buffer
+                ok = __all_sync(0xffffffffu, mbar_wait(&empty[s], (uint32_t)((k / kStages - 1) & 1)));
+                if (!ok) break;
+                if (!BETA) unstage_tile<S>(a, blockIdx.x + (k - kStages) * stride, stage, lane);
+            }
+            if (k < mine) stage_tile<S, BETA>(a, blockIdx.x + k * stride, stage, &full[s], lane);
+        }
+        if (!ok && lane == 0) atomicOr(&g_stage_error, kStageTimeout);
+        bulk_wait_all();
+        return;
+    }
+
+    for (int k = 0; k < mine; ++k) {  // compute warps
+        const int s = k % kStages;
+        unsigned char *stage = buf + s * TL::STAGE;
+        if (!mbar_wait(&full[s], (uint32_t)((k / kStages) & 1))) {
+            if (lane == 0) atomicOr(&g_stage_error, kStageTimeout);
+            break;
+        }
+        const int t = blockIdx.x + k * stride;
+        const LatDesc &d = lattice_of_unit(a, t);
+        const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
+        if (BETA && !beta_tile_inside<S>(d, c0)) {
+#pragma unroll 1
+            for (int m = 0; m < TL::PER; m++) {
+                const int64_t c = c0 + threadIdx.x + 32 * kConsumerWarps * m;
+                if (c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+            }
+        } else {
+#pragma unroll 1
+            for (int m = 0; m < TL::PER; m++) {
+                const int l = threadIdx.x + 32 * kConsumerWarps * m;
+                const int64_t c = c0 + l;
+                if (c >= d.n) break;
+                if (BETA) beta_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
+                else alpha_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
+            }
+        }
+        if (!BETA) fence_async_smem();  // the bulk stores read what this warp wrote
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
+}
+
 // ------------------------------------------------ batches of lattices
 // Every lattice of a batch keeps its own step counter: step j of a tick is
 // a beta step for a lattice whose counter was even at the tick start and j
 // even (and so on), chosen per block.  Used for ensembles of cavities and
 // for the serving loop, where solves start at different times.
-// k_step holds both kernels' code: without the subgrid model it takes the
-// alpha kernel's register budget.
 template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES, LES>())) k_step(const __grid_constant__ BatchArgs a, int j) {
+__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_step(const __grid_constant__ BatchArgs a, int j) {
     const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
