@@ -102,13 +102,17 @@ int lbm_cu_perturb(lbm_lattice *lat, const int origin[3], const int phys[3], uin
  * CLbmSolver::simulationStep (src/CLbmSolver.hpp:664-676). */
 int lbm_cu_step(lbm_lattice *lat, int parity, void *stream);
 
-/* Kernel shape of the step: 1 (default) is one cell per thread; 2 processes
- * two neighbouring x cells per thread with 64-bit accesses (32-bit for 16-bit
- * storage) where the arithmetic type is float and nx is even, else falls back
- * to 1.  Both shapes give bit-identical results; on GB300 the one-cell shape
- * is faster for the sizes measured (more resident warps).  No reference counterpart (the
- * reference's work-group size list, src/CLbmSolver.hpp:279-312, tunes its
- * OpenCL launch instead). */
+/* Kernel shape of the step.  1: one cell per thread.  2: two neighbouring x
+ * cells per thread with 64-bit accesses (32-bit for 16-bit storage) where the
+ * arithmetic type is float and nx is even, else 1.  3: persistent blocks
+ * that stream tiles of cells through shared memory with TMA bulk copies (a
+ * producer warp keeps the next tiles in flight while eight warps compute);
+ * float, half and bfloat16 storage, else 1; the beta step of a lattice whose
+ * nx is not a multiple of 16 bytes of populations runs shape 1.  0
+ * (default): 3 for half and bfloat16 storage, 1 for float and double, the
+ * fastest measured on GB300.  All shapes give bit-identical results.  No
+ * reference counterpart (the reference's work-group size list,
+ * src/CLbmSolver.hpp:279-312, tunes its OpenCL launch instead). */
 int lbm_cu_set_kernel_shape(lbm_lattice *lat, int cells_per_thread);
 
 /* Rectangular copy of one field between the lattice and a HOST buffer laid

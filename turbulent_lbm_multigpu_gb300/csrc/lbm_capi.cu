@@ -421,6 +421,7 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab) {
 }
 
 int effective_shape(int storage, int shape, const LatDesc *tab, int ntab) {
+    if (shape == 0) shape = (storage == kF16 || storage == kBF16) ? 3 : 1;  // the measured best per storage
     if (shape == 2 && pair_shape(storage, tab, ntab)) return 2;
     if (shape == 3 && storage != kF64) return 3;
     return 1;
@@ -940,7 +941,7 @@ struct lbm_domain {
     std::vector<std::vector<int>> bc;
     std::vector<int> coords;  // 3 per subdomain
     std::vector<LatDesc> h_tab;  // descriptors of the subdomains
-    int shape = 1;               // requested kernel shape
+    int shape = 0;               // requested kernel shape (0: per storage type)
     int eff_shape = 1;           // the shape the subdomains run
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
@@ -1234,14 +1235,14 @@ int lbm_cu_domain_set_store_interval(lbm_domain *D, int interval) {
 
 int lbm_cu_set_kernel_shape(lbm_lattice *l, int cells_per_thread) {
     if (!l) return fail("NULL lattice");
-    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("kernel shape is 1, 2 or 3");
+    if (cells_per_thread < 0 || cells_per_thread > 3) return fail("kernel shape is 0 (automatic), 1, 2 or 3");
     l->shape = cells_per_thread;
     return 0;
 }
 
 int lbm_cu_domain_set_kernel_shape(lbm_domain *D, int cells_per_thread) {
     if (!D) return fail("NULL domain");
-    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("kernel shape is 1, 2 or 3");
+    if (cells_per_thread < 0 || cells_per_thread > 3) return fail("kernel shape is 0 (automatic), 1, 2 or 3");
     D->shape = cells_per_thread;
     D->tab_dirty = true;
     drop_graph(D);

@@ -40,7 +40,8 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab);
 inline int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
 
 // Kernel shapes of a step: 1 one cell per thread, 2 two cells per thread,
-// 3 tiles staged through shared memory by bulk copies.
+// 3 tiles staged through shared memory by bulk copies, 0 automatic (3 for
+// the 16-bit storage types, 1 otherwise: the fastest measured on GB300).
 // The shape a set of lattices runs: 2 needs float arithmetic and even nx,
 // 3 float/half/bfloat16 storage; otherwise 1.
 int effective_shape(int storage, int shape, const LatDesc *tab, int ntab);
@@ -65,5 +66,5 @@ struct lbm_lattice {
     bool dirty = true;
     void *stage = nullptr;  // staging for host copies and reduction partials
     size_t stage_bytes = 0;
-    int shape = 1;  // requested kernel shape (tuning option, see effective_shape)
+    int shape = 0;  // requested kernel shape (0: per storage type, see effective_shape)
 };

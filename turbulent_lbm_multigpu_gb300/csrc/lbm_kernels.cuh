@@ -950,7 +950,7 @@ template <typename S> struct Tile {
     static_assert(sizeof(S) <= 4, "staged tiles hold float, half or bfloat16 populations");
     static constexpr int T = 1024 / (int)sizeof(S);  // cells per tile: 1 KB per plane
     static constexpr int A = 128 / (int)sizeof(S);   // elements per 128-byte line
-    static constexpr int PER = T / (32 * kConsumerWarps);  // cells per compute thread
+    static constexpr int PER = (T + 32 * kConsumerWarps - 1) / (32 * kConsumerWarps);  // cells per compute thread
     static constexpr int SEG = (T + A) * (int)sizeof(S);   // bytes per plane segment
     static constexpr int STAGE = 19 * SEG + T;       // 19 segments + flag bytes
     static constexpr int SMEM = 128 + kStages * STAGE;  // barriers + the ring
@@ -1173,15 +1173,16 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
         if (BETA && !beta_tile_inside<S>(d, c0)) {
 #pragma unroll 1
             for (int m = 0; m < TL::PER; m++) {
-                const int64_t c = c0 + threadIdx.x + 32 * kConsumerWarps * m;
-                if (c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
+                const int l = threadIdx.x + 32 * kConsumerWarps * m;
+                const int64_t c = c0 + l;
+                if (l < TL::T && c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
             }
         } else {
 #pragma unroll 1
             for (int m = 0; m < TL::PER; m++) {
                 const int l = threadIdx.x + 32 * kConsumerWarps * m;
                 const int64_t c = c0 + l;
-                if (c >= d.n) break;
+                if (l >= TL::T || c >= d.n) break;
                 if (BETA) beta_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
                 else alpha_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
             }
