@@ -377,8 +377,6 @@ def run_e2e(api, prm, steps):
     D = api.Domain(SIZE, NUMS, api.F32, store_velocity=True, store_density=False)
     D.set_params(prm)
     D.set_halo_mode(HALO_MODE)
-    if shape:
-        D.set_kernel_shape(shape)
     D.reset()
     D.perturb(SEED, AMP)
     D.set_store_interval(0)  # velocity written on the last step only

@@ -166,6 +166,17 @@ int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int la
  * overlaps on the GPU race and must be ordered by the caller. */
 int lbm_cu_reduce_conserved_noalloc(lbm_lattice *lat, int layout, double out[5], void *stream);
 
+/* Checkpoint / restart (no reference counterpart: the reference writes VTK
+ * snapshots only).  The file holds the lattice's raw stored populations
+ * (bit for bit, any storage type), its flags and `counter`, the step counter
+ * of the caller; the counter's parity is the A-A slot layout of the stored
+ * populations (odd after an alpha step), so restarting with the returned
+ * counter continues the exact kernel sequence: the results are identical to
+ * an uninterrupted run.  Load checks the size and storage type and an FNV-1a
+ * hash of the data.  Both synchronise `stream` first and block. */
+int lbm_cu_checkpoint_save(lbm_lattice *lat, const char *path, int64_t counter, void *stream);
+int lbm_cu_checkpoint_load(lbm_lattice *lat, const char *path, int64_t *counter, void *stream);
+
 /* ----------------------------------------------------------------- domain */
 
 /* A decomposed domain held on one GPU: the even split and CComm geometry of
@@ -210,6 +221,13 @@ int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launch
 int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
 int lbm_cu_domain_subdomains(const lbm_domain *dom, int *count, int sub_size[3]);
 lbm_lattice *lbm_cu_domain_lattice(lbm_domain *dom, int index);
+
+/* Checkpoint / restart of a whole decomposed domain: every subdomain's raw
+ * populations and flags and the domain's step counter, which load restores
+ * (see lbm_cu_checkpoint_save).  The domain must have the same size,
+ * decomposition and storage type. */
+int lbm_cu_domain_checkpoint_save(lbm_domain *dom, const char *path, void *stream);
+int lbm_cu_domain_checkpoint_load(lbm_domain *dom, const char *path, void *stream);
 
 /* ------------------------------------------------------ batches, serving */
 

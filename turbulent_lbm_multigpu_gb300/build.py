@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
            "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CU_SOURCES = ["lbm_capi.cu", "lbm_batch.cu"]
+CU_SOURCES = ["lbm_capi.cu", "lbm_batch.cu", "lbm_io.cu"]
 
 
 def nvcc() -> str:

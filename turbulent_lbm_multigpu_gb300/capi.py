@@ -105,6 +105,10 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
         "lbm_cu_domain_lattice": ([vp, ci], vp),
         "lbm_cu_run": ([vp, i64, i64, vp], ci),
+        "lbm_cu_checkpoint_save": ([vp, C.c_char_p, i64, vp], ci),
+        "lbm_cu_checkpoint_load": ([vp, C.c_char_p, C.POINTER(i64), vp], ci),
+        "lbm_cu_domain_checkpoint_save": ([vp, C.c_char_p, vp], ci),
+        "lbm_cu_domain_checkpoint_load": ([vp, C.c_char_p, vp], ci),
         "lbm_cu_batch_create": ([C.POINTER(Cavity), ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_batch_destroy": ([vp], ci),
         "lbm_cu_batch_reset": ([vp, vp], ci),
@@ -225,6 +229,16 @@ class Lattice:
         check(lib().lbm_cu_reduce_conserved(self.h, layout, out, stream))
         return np.array(out[:], dtype=np.float64)
 
+    def checkpoint_save(self, path, counter: int, stream=None):
+        """Raw populations, flags and the step counter to a file (restart is bit-exact)."""
+        check(lib().lbm_cu_checkpoint_save(self.h, str(path).encode(), int(counter), stream))
+
+    def checkpoint_load(self, path, stream=None) -> int:
+        """Restore a checkpoint of a lattice of the same size and storage; returns its step counter."""
+        c = C.c_int64()
+        check(lib().lbm_cu_checkpoint_load(self.h, str(path).encode(), C.byref(c), stream))
+        return c.value
+
     def reduce_conserved_noalloc(self, layout: int, stream=None):
         """The same sums without any device allocation (fixed in-library
         scratch, lattices up to 512^3 cells); see include/lbm_gb300.h."""
@@ -299,6 +313,13 @@ class Domain:
 
     def set_store_interval(self, interval: int):
         check(lib().lbm_cu_domain_set_store_interval(self.h, interval))
+
+    def checkpoint_save(self, path, stream=None):
+        check(lib().lbm_cu_domain_checkpoint_save(self.h, str(path).encode(), stream))
+
+    def checkpoint_load(self, path, stream=None):
+        """Restore every subdomain and the step counter."""
+        check(lib().lbm_cu_domain_checkpoint_load(self.h, str(path).encode(), stream))
 
     def set_kernel_shape(self, cells_per_thread: int):
         check(lib().lbm_cu_domain_set_kernel_shape(self.h, cells_per_thread))

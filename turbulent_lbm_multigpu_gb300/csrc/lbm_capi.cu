@@ -1297,6 +1297,67 @@ int lbm_cu_domain_subdomains(const lbm_domain *D, int *count, int sub_size[3]) {
     return 0;
 }
 
+// Domain checkpoint: a header with the decomposition and the step counter,
+// then every subdomain's lattice block (lbm_io.cu).
+namespace {
+struct DomHeader {
+    char magic[8];
+    int32_t storage;
+    int32_t size[3], nums[3];
+    int32_t reserved;
+    int64_t counter;
+};
+static_assert(sizeof(DomHeader) == 48, "domain checkpoint header layout");
+constexpr char kDomMagic[8] = {'L', 'B', 'M', 'D', 'C', 'K', 'P', '1'};
+struct FileCloser {
+    FILE *f;
+    ~FileCloser() {
+        if (f) fclose(f);
+    }
+};
+}  // namespace
+
+int lbm_cu_domain_checkpoint_save(lbm_domain *D, const char *path, void *stream) {
+    if (!D || !path) return fail("NULL argument");
+    CU(cudaStreamSynchronize(S(stream)));
+    FileCloser fc{fopen(path, "wb")};
+    if (!fc.f) return fail(std::string("cannot open ") + path + " for writing");
+    DomHeader hd{};
+    memcpy(hd.magic, kDomMagic, 8);
+    hd.storage = D->storage;
+    for (int a = 0; a < 3; a++) {
+        hd.size[a] = D->size[a];
+        hd.nums[a] = D->nums[a];
+    }
+    hd.counter = D->counter;
+    if (fwrite(&hd, sizeof(hd), 1, fc.f) != 1) return fail("checkpoint write failed");
+    for (auto *l : D->subs)
+        if (ckpt_write_lattice(fc.f, l, D->counter)) return -1;
+    if (fflush(fc.f)) return fail("checkpoint write failed");
+    return 0;
+}
+
+int lbm_cu_domain_checkpoint_load(lbm_domain *D, const char *path, void *stream) {
+    if (!D || !path) return fail("NULL argument");
+    CU(cudaStreamSynchronize(S(stream)));
+    FileCloser fc{fopen(path, "rb")};
+    if (!fc.f) return fail(std::string("cannot open ") + path);
+    DomHeader hd{};
+    if (fread(&hd, sizeof(hd), 1, fc.f) != 1) return fail("checkpoint file is truncated");
+    if (memcmp(hd.magic, kDomMagic, 8)) return fail("not a domain checkpoint (bad magic)");
+    if (hd.storage != D->storage) return fail("checkpoint storage type does not match");
+    for (int a = 0; a < 3; a++)
+        if (hd.size[a] != D->size[a] || hd.nums[a] != D->nums[a])
+            return fail("checkpoint decomposition does not match");
+    for (auto *l : D->subs) {
+        int64_t c = 0;
+        if (ckpt_read_lattice(fc.f, l, &c)) return -1;
+        if (c != hd.counter) return fail("checkpoint subdomain counters disagree");
+    }
+    D->counter = hd.counter;
+    return 0;
+}
+
 lbm_lattice *lbm_cu_domain_lattice(lbm_domain *D, int index) {
     if (!D || index < 0 || index >= (int)D->subs.size()) {
         fail("subdomain index out of range");

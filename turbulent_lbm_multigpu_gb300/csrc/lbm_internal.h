@@ -1,6 +1,7 @@
 // lbm_internal.h -- host runtime shared by the translation units of
 // liblbm_gb300.so (not part of the public C ABI).
 #pragma once
+#include <cstdio>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -50,6 +51,9 @@ int effective_shape(int storage, int shape, const LatDesc *tab, int ntab);
 // descriptors per launch.
 int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
                 cudaStream_t st);
+// One lattice block of a checkpoint file (lbm_io.cu).
+int ckpt_write_lattice(FILE *f, lbm_lattice *l, int64_t counter);
+int ckpt_read_lattice(FILE *f, lbm_lattice *l, int64_t *counter);
 }  // namespace lbm_rt
 
 struct lbm_lattice {
