@@ -104,6 +104,14 @@ public:
     std::list<int> lbm_opencl_number_of_registers_list;
     std::list<int> lbm_opencl_number_of_threads_list;
     bool debug_mode = false;
+    // append the timing of each run to output/benchmark/benchmark_<subdomains>.ini
+    // (the reference's BENCHMARK build, src/CController.hpp:445-477); a build with
+    // -DBENCHMARK=1 turns it on by default, the command line with -b
+#if defined(BENCHMARK) && BENCHMARK
+    bool benchmark = true;
+#else
+    bool benchmark = false;
+#endif
 
     // optional lattice-unit additions
     bool lattice_units = false;

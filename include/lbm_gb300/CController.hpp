@@ -21,11 +21,28 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "CComm.hpp"
 #include "CConfiguration.hpp"
 #include "CDomain.hpp"
 #include "CLbmSolver.hpp"
+#include "CLbmVisualizationVTK.hpp"
 #include "CStopwatch.hpp"
+
+// output folders of the reference (src/common.h:26-28)
+#ifndef BENCHMARK_OUTPUT_DIR
+#define BENCHMARK_OUTPUT_DIR "output/benchmark"
+#endif
+#ifndef VTK_OUTPUT_DIR
+#define VTK_OUTPUT_DIR "output/vtk"
+#endif
+
+// mkdir -p
+inline void lbm_make_dirs(const std::string &path) {
+    for (size_t i = 1; i <= path.size(); i++)
+        if (i == path.size() || path[i] == '/') mkdir(path.substr(0, i).c_str(), 0755);
+}
 
 template <typename T>
 using ConfigSingletonT = Singleton<CConfiguration<T>>;
@@ -131,30 +148,75 @@ public:
         else syncAlpha();
     }
 
-    /** The time loop of one subdomain and its report (src/CController.hpp:396-522). */
+    /** The time loop of one subdomain and its report (src/CController.hpp:396-522):
+     *  with visualization on, a VTK snapshot ./output/vtk/OUTPUT.<UID>.<step>.vtk
+     *  after every step. */
     int run() {
         CConfiguration<T> *cfg = ConfigSingletonT<T>::Instance();
         int loops = cfg->loops < 0 ? 100 : cfg->loops;
+        CLbmVisualizationVTK<T> *vis = nullptr;
+        if (cfg->do_visualization) vis = newVisualization();
         CStopwatch sw;
         sw.start();
-        for (int i = 0; i < loops; i++) computeNextStep();
+        for (int i = 0; i < loops; i++) {
+            computeNextStep();
+            if (vis) vis->render(i);
+        }
         cLbmPtr->wait();
         sw.stop();
+        delete vis;  // waits for the last snapshots
+        benchmarkRecord(loops, sw.time, cfg->do_visualization || cfg->debug_mode);
         report(_domain.getSize(), loops, sw.time, cfg->do_visualization || cfg->debug_mode);
         return 0;
     }
 
+    /** A VTK writer of this subdomain into ./output/vtk (created if missing). */
+    CLbmVisualizationVTK<T> *newVisualization() {
+        lbm_make_dirs(VTK_OUTPUT_DIR);
+        auto *vis = new CLbmVisualizationVTK<T>(_UID, std::string("./") + VTK_OUTPUT_DIR + "/OUTPUT");
+        vis->setup(cLbmPtr);
+        return vis;
+    }
+
+    /** The console report of a run (src/CController.hpp:478-510). */
     static void report(CVector<3, int> cube, int loops, double seconds, bool vis) {
         double floats_per_cell = 19.0 * 2.0 + 1.0 + (vis ? 3.0 : 0.0);
+        double fps = ((double)loops) / seconds;
+        double mlups = ((double)fps * (double)cube.elements()) * (double)0.000001;
         std::cout << std::endl << "Cube: " << cube << std::endl;
         std::cout << "Seconds: " << seconds << std::endl;
-        double fps = ((double)loops) / seconds;
         std::cout << "FPS: " << fps << std::endl;
-        double mlups = ((double)fps * (double)cube.elements()) * (double)0.000001;
         std::cout << "MLUPS: " << mlups << std::endl;
         std::cout << "Bandwidth: " << (mlups * floats_per_cell * (double)sizeof(T)) << " MB/s (RW, bidirectional)"
                   << std::endl;
         std::cout << "done." << std::endl;
+    }
+
+    /** With cfg->benchmark, the record of the reference's BENCHMARK build
+     *  (src/CController.hpp:445-477): the whole configured domain's timing
+     *  appended to output/benchmark/benchmark_<number of subdomains>.ini. */
+    static void benchmarkRecord(int loops, double seconds, bool vis) {
+        CConfiguration<T> *cfg = ConfigSingletonT<T>::Instance();
+        if (!cfg->benchmark) return;
+        const double floats_per_cell = 19.0 * 2.0 + 1.0 + (vis ? 3.0 : 0.0);
+        const double fps = ((double)loops) / seconds;
+        const double mlups = fps * (double)cfg->domain_size.elements() * 0.000001;
+        lbm_make_dirs(BENCHMARK_OUTPUT_DIR);
+        std::stringstream name;
+        name << "./" << BENCHMARK_OUTPUT_DIR << "/benchmark_" << cfg->subdomain_num.elements() << ".ini";
+        std::ofstream f(name.str().c_str(), std::ios::out | std::ios::app);
+        if (!f.is_open()) {
+            std::cout << "Unable to open file";
+            return;
+        }
+        f << "CUBE_X : " << cfg->domain_size[0] << std::endl;
+        f << "CUBE_Y : " << cfg->domain_size[1] << std::endl;
+        f << "CUBE_Z : " << cfg->domain_size[2] << std::endl;
+        f << "SECONDS : " << seconds << std::endl;
+        f << "FPS : " << fps << std::endl;
+        f << "MLUPS : " << mlups << std::endl;
+        f << "BANDWIDTH : " << (mlups * floats_per_cell * (double)sizeof(T)) << std::endl;
+        f << std::endl;
     }
 
     void addCommunication(CComm<T> *comm) { _comm_container.push_back(comm); }

@@ -93,15 +93,26 @@ public:
             }
     }
 
+    /** All subdomains' time loops in lock-step and the report of the whole
+     *  domain; with visualization on, every subdomain writes its VTK snapshot
+     *  after every step, as each reference rank does. */
     void startSimulation() {
         if (_controllers.empty()) throw "CManager: Initialize the simulation before starting it!";
         CConfiguration<T> *cfg = ConfigSingletonT<T>::Instance();
         int loops = cfg->loops < 0 ? 100 : cfg->loops;
+        std::vector<CLbmVisualizationVTK<T> *> vis;
+        if (cfg->do_visualization)
+            for (auto *c : _controllers) vis.push_back(c->newVisualization());
         CStopwatch sw;
         sw.start();
-        for (int i = 0; i < loops; i++) step();
+        for (int i = 0; i < loops; i++) {
+            step();
+            for (auto *v : vis) v->render(i);
+        }
         for (auto *c : _controllers) c->getSolver()->wait();
         sw.stop();
+        for (auto *v : vis) delete v;  // waits for the last snapshots
+        CController<T>::benchmarkRecord(loops, sw.time, cfg->do_visualization || cfg->debug_mode);
         CController<T>::report(_domain.getSize(), loops, sw.time, cfg->do_visualization || cfg->debug_mode);
     }
 

@@ -1,11 +1,15 @@
 // host_probe.cpp -- test driver for the host-side C++ headers (no GPU):
 //   host_probe conf <file>      parse conf.xml, print the fields
 //   host_probe skeleton         CLbmSkeleton<float> of the reference defaults
+//   host_probe vtk <file> <threads> <nx> <ny> <nz>   a VTK file of a synthetic subdomain
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "lbm_gb300/CConfiguration.hpp"
 #include "lbm_gb300/CLbmSkeleton.hpp"
+#include "lbm_gb300/VTK_Common.hpp"
 
 int main(int argc, char **argv) {
     if (argc >= 3 && !strcmp(argv[1], "conf")) {
@@ -42,6 +46,21 @@ int main(int argc, char **argv) {
                s.d_timestep, s.gravitation[0], s.gravitation[1], s.gravitation[2], s.drivenCavityVelocity[0],
                s.d_reynolds, (int)s.error());
         return 0;
+    }
+    if (argc >= 7 && !strcmp(argv[1], "vtk")) {
+        const int nx = atoi(argv[4]), ny = atoi(argv[5]), nz = atoi(argv[6]), n = nx * ny * nz;
+        std::vector<float> rho(n), vel(3 * n);
+        std::vector<int> fl(n);
+        for (int a = 0; a < n; a++) {
+            rho[a] = 1.0f + 0.001f * (float)a - 0.0375f * (float)(a % 7);
+            fl[a] = 1 << (a % 4);
+            vel[a] = 0.01f * (float)((a * 37) % 101 - 50) / 7.0f;
+            vel[n + a] = -0.02f * (float)(a % 5) / 3.0f;
+            vel[2 * n + a] = 1e-7f * (float)a;
+        }
+        const bool ok = lbm_vtk::write_vtk_cells<float>(argv[2], nx, ny, nz, 0.1f / 32.0f, CVector<3, int>(2, 0, 6),
+                                                        rho.data(), fl.data(), vel.data(), (unsigned)atoi(argv[3]));
+        return ok ? 0 : 4;
     }
     return 1;
 }

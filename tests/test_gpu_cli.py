@@ -1,0 +1,60 @@
+"""The command-line driver (CManager / CController over the C ABI) with the
+reference's output options: VTK snapshots after every step (-g) and the
+benchmark .ini record (-b)."""
+from __future__ import annotations
+
+import configparser
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def parse_vtk(path):
+    lines = path.read_text().splitlines()
+    assert lines[:3] == ["# vtk DataFile Version 3.1", "Turbulent Fluid Simulation on MultiGPU.", "ASCII"]
+    assert lines[4] == "DATASET STRUCTURED_GRID"
+    dims = [int(v) for v in lines[5].split()[1:]]
+    npts = int(lines[6].split()[1])
+    assert npts == dims[0] * dims[1] * dims[2]
+    at = 8 + npts + 1
+    ncell = int(lines[at].split()[1])
+    rho = np.array(lines[at + 3:at + 3 + ncell], dtype=np.float64)
+    at += 3 + ncell + 1
+    assert lines[at] == "SCALARS flag INT 1 "
+    flags = np.array(lines[at + 2:at + 2 + ncell], dtype=np.int64)
+    at += 2 + ncell + 1
+    assert lines[at] == "VECTORS velocity float"
+    vel = np.array([ln.split() for ln in lines[at + 1:at + 1 + ncell]], dtype=np.float64)
+    return [d - 1 for d in dims], rho, flags, vel
+
+
+def test_cli_writes_vtk_snapshots_and_benchmark_record(capi, tmp_path):
+    exe = ROOT / "turbulent_lbm_multigpu_gb300" / "lbm_gb300"
+    out = subprocess.run([str(exe), "-x", "16", "-y", "16", "-z", "16", "-X", "2", "-l", "3", "-g", "-b"],
+                         cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "MLUPS:" in out.stdout
+    for uid in (0, 1):
+        for step in range(3):
+            assert (tmp_path / "output" / "vtk" / f"OUTPUT.{uid}.{step}.vtk").exists()
+    dims, rho, flags, vel = parse_vtk(tmp_path / "output" / "vtk" / "OUTPUT.0.2.vtk")
+    assert dims == [8, 16, 16]
+    f = flags.reshape(16, 16, 8)  # z, y, x
+    # subdomain 0 of a 2x1x1 split: walls at x = 0 and on the y / z faces,
+    # the ghost layer at x = 7, the lid plane y = 14 (x in [1, 6], z in [1, 14])
+    assert (f[:, :, 0] == 1).all() and (f[1:-1, 1:-1, 7] == 8).all()
+    assert (f[1:-1, 14, 1:7] == 4).all() and (f[1:-1, 1:14, 1:7] == 2).all()
+    assert np.isfinite(rho).all() and np.isfinite(vel).all()
+    assert np.abs(vel[f.reshape(-1) == 4, 0]).max() > 0  # the lid moves
+    ini = configparser.ConfigParser()
+    text = (tmp_path / "output" / "benchmark" / "benchmark_2.ini").read_text()
+    ini.read_string("[EXP1]\n" + text)
+    e = ini["EXP1"]
+    assert (int(e["CUBE_X"]), int(e["CUBE_Y"]), int(e["CUBE_Z"])) == (16, 16, 16)
+    assert float(e["MLUPS"]) > 0 and float(e["SECONDS"]) > 0 and float(e["FPS"]) > 0

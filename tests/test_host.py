@@ -158,3 +158,59 @@ def test_bench_multirank_aggregation_gloo():
         p.join(60)
     assert [r[1] for r in res] == [11.0, 11.0]
     assert res[0][2] == pytest.approx(1000 * 4 * 2 / 11e-3 / 1e6)
+
+
+def _vtk_expected(nx, ny, nz):
+    """The reference's VTK text (src/libvis/CLbmVisualizationVTK.hpp:27-99 and
+    VTK_Common.hpp:31-46) for the probe's synthetic subdomain, built in
+    float32 like the C++ writer and printed with C's %f."""
+    f = np.float32
+    n = nx * ny * nz
+    a = np.arange(n)
+    rho = (f(1.0) + f(0.001) * a.astype(f) - f(0.0375) * (a % 7).astype(f)).astype(f)
+    vx = (f(0.01) * ((a * 37) % 101 - 50).astype(f) / f(7.0)).astype(f)
+    vy = (f(-0.02) * (a % 5).astype(f) / f(3.0)).astype(f)
+    vz = (f(1e-7) * a.astype(f)).astype(f)
+    fl = 1 << (a % 4)
+    dx = f(0.1) / f(32.0)
+    ox, oy, oz = f(2) * dx, f(0) * dx, f(6) * dx
+    out = ["# vtk DataFile Version 3.1\n", "Turbulent Fluid Simulation on MultiGPU.\n", "ASCII\n", "\n",
+           "DATASET STRUCTURED_GRID\n", f"DIMENSIONS  {nx + 1} {ny + 1} {nz + 1} \n",
+           f"POINTS {(nx + 1) * (ny + 1) * (nz + 1)} float\n", "\n"]
+    for k in range(nz + 1):
+        for j in range(ny + 1):
+            for i in range(nx + 1):
+                out.append("%f %f %f\n" % (float(f(ox + f(i) * dx)), float(f(oy + f(j) * dx)), float(f(oz + f(k) * dx))))
+    out += ["\n", f"CELL_DATA {n} \n", "SCALARS density float 1 \n", "LOOKUP_TABLE default \n"]
+    out += ["%f\n" % float(v) for v in rho]
+    out += ["\n", "SCALARS flag INT 1 \n", "LOOKUP_TABLE default \n"]
+    out += ["%i\n" % int(v) for v in fl]
+    out += ["\n", "VECTORS velocity float\n"]
+    out += ["%f %f %f\n" % (float(x), float(y), float(z)) for x, y, z in zip(vx, vy, vz)]
+    return "".join(out)
+
+
+@pytest.mark.parametrize("threads,dims", [(1, (5, 4, 3)), (3, (40, 30, 20))])
+def test_vtk_writer_matches_reference_layout(probe, tmp_path, threads, dims):
+    """Byte-identical to the reference's serial fprintf output, also when the
+    text is formatted by several threads (the 40x30x20 case splits every
+    section)."""
+    path = tmp_path / "OUTPUT.0.1.vtk"
+    subprocess.run([str(probe), "vtk", str(path), str(threads), *map(str, dims)], check=True)
+    assert path.read_text() == _vtk_expected(*dims)
+
+
+def test_scaling_records_follow_the_reference_layout(tmp_path):
+    """The sweep's .ini records and their analysis (benchmark.py analyse():
+    averages per key over the [EXPn] sections, keyed by NP)."""
+    from turbulent_lbm_multigpu_gb300 import scaling
+
+    p = tmp_path / "benchmark_4.ini"
+    scaling.append_record(p, 1, 4, (256, 256, 256), 2.0, 100, 4)
+    scaling.append_record(p, 2, 4, (256, 256, 256), 4.0, 100, 4)
+    text = p.read_text()
+    assert text.startswith("[EXP1]\nNP : 4\nCUBE_X : 256\n")
+    r = scaling.analyse([str(p)])[4]
+    assert r["SECONDS"] == pytest.approx(3.0) and r["FPS"] == pytest.approx(37.5)
+    assert r["MLUPS"] == pytest.approx(37.5 * 256 ** 3 * 1e-6)
+    assert r["BANDWIDTH"] == pytest.approx(r["MLUPS"] * 39 * 4)

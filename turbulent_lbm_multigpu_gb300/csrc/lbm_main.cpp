@@ -41,7 +41,8 @@ static int usage(const char *argv0) {
               << "\t\t[-d device_num]\n\t\t[-k number of kernels to run ]\n\t\t[-g]\t(VTK output flag)\n"
               << "\t\t[-R registers list]\t[-T work group threads list]\n"
               << "\t\t[-t timestep]\t(default: -1 for automatic detection)\n"
-              << "    \t[-u] run unit tests\n    \t[-c] read the configuration file" << std::endl;
+              << "    \t[-u] run unit tests\n    \t[-c] read the configuration file\n"
+              << "    \t[-b] append the timing to output/benchmark/benchmark_<subdomains>.ini" << std::endl;
     return -1;
 }
 
@@ -52,11 +53,11 @@ int main(int argc, char **argv) {
     CVector<4, T> cavity(100, 0, 0, 1);
     T viscosity = 0.001308f, timestep = -1.0f;
     int loops = -1, device_nr = 0;
-    bool do_vis = false, unit_test = false, use_conf = false;
+    bool do_vis = false, unit_test = false, use_conf = false, benchmark = false;
     size_t kernel_count = 128;
     std::string regs, threads, conf_file;
     int ch;
-    while ((ch = getopt(argc, argv, "x:y:z:d:vr:k:gG:t:sl:R:T:X:Y:Z:S:u:c:n:m:p:")) > 0) {
+    while ((ch = getopt(argc, argv, "x:y:z:d:vr:k:gG:t:sl:R:T:X:Y:Z:S:u:c:n:m:p:b")) > 0) {
         switch (ch) {
             case 'd': device_nr = atoi(optarg); break;
             case 'v': debug = true; break;
@@ -81,6 +82,7 @@ int main(int argc, char **argv) {
             case 's': break;
             case 'u': unit_test = true; break;
             case 'c': use_conf = true; conf_file = optarg; break;
+            case 'b': benchmark = true; break;
             default: return usage(argv[0]);
         }
     }
@@ -104,6 +106,7 @@ int main(int argc, char **argv) {
             if (!regs.empty()) extract_comma_separated_integers(cfg->lbm_opencl_number_of_registers_list, regs);
         }
         cfg->debug_mode = debug;
+        if (benchmark) cfg->benchmark = true;
         if (debug) cfg->printMe();
         if (unit_test) {
             std::cout << "no unit tests are registered" << std::endl;
