@@ -52,6 +52,12 @@ typedef struct lbm_params {
     double les_c;
     double gravity[3];
     double lid;
+    /* 0: the reference's alpha forcing, whose temporary aliases rho
+     * (lbm_alpha.cl:173): the term of pair k is coefficient k times the term of
+     * pair k-1, and the stored density is the last term.  1: each pair's term
+     * is its coefficient times the density, and the stored density is the
+     * density (not the reference's results; off by default). */
+    int32_t gravity_mode;
 } lbm_params;
 
 typedef struct lbm_lattice lbm_lattice; /* one subdomain's device fields */

@@ -38,6 +38,7 @@ struct CLbmOptions {
     bool lattice_units = false; // take tau and the lid speed below as given
     T lattice_tau = T(0);
     T lattice_lid = T(0);
+    int gravity_mode = 0;       // 1: per-term gravity forcing instead of the reference's (lbm_params)
 };
 
 /** D3Q19 direction vectors in reference order (src/main.cpp:38-66). */
@@ -81,6 +82,7 @@ private:
         p.les_c = (double)(T)(18.0 * std::sqrt(2.0) * (double)opt.smagorinsky * (double)opt.smagorinsky);
         for (int a = 0; a < 3; a++) p.gravity[a] = this->gravitation[a];
         p.lid = lid;
+        p.gravity_mode = opt.gravity_mode;
         return p;
     }
     int o3(const CVector<3, int> &v, int out[3]) const {
@@ -172,6 +174,29 @@ public:
     }
     void wait() {
         if (lbm_cu_synchronize(ctx.stream)) fail("wait");
+    }
+
+    /** Restart file of this subdomain: raw populations, flags and
+     *  simulation_step_counter (lbm_cu_checkpoint_save; no reference
+     *  counterpart).  false (and the error sink) on failure. */
+    bool saveCheckpoint(const std::string &path) {
+        if (lbm_cu_checkpoint_save(lat, path.c_str(), (int64_t)simulation_step_counter, ctx.stream)) {
+            fail("checkpoint save");
+            return false;
+        }
+        return true;
+    }
+    /** Restores a checkpoint of a subdomain of the same size and storage,
+     *  including simulation_step_counter, so the next simulationStep() runs
+     *  the kernel the interrupted run would have run. */
+    bool loadCheckpoint(const std::string &path) {
+        int64_t c = 0;
+        if (lbm_cu_checkpoint_load(lat, path.c_str(), &c, ctx.stream)) {
+            fail("checkpoint load");
+            return false;
+        }
+        simulation_step_counter = (size_t)c;
+        return true;
     }
 
     // ---------------------------------------------------------- transfers

@@ -243,8 +243,21 @@ static void collide(REAL f[19], REAL rho, REAL vx, REAL vy, REAL vz, REAL dp, RE
 /* The alpha kernel's gravity terms.  The reference aliases its temporary to
  * rho (lbm_alpha.cl:173), so each pair's force term is the previous term
  * times the next coefficient and the stored density is the last term.
- * t[k] is added to f[2k] and subtracted from f[2k+1]. */
-static REAL gravity_chain(REAL rho, REAL gx, REAL gy, REAL gz, REAL t[9]) {
+ * t[k] is added to f[2k] and subtracted from f[2k+1].  gmode 1 is the
+ * optional per-term forcing: term k = coefficient k times the density. */
+static REAL gravity_chain(REAL rho, REAL gx, REAL gy, REAL gz, REAL t[9], int gmode) {
+    if (gmode) { /* per-term forcing (not the reference's): coefficient k times the density */
+        t[0] = gx * C18 * rho;
+        t[1] = gy * ((REAL)(-1.0f / 18.0f)) * rho;
+        t[2] = (gx - gy) * C36 * rho;
+        t[3] = (gx + gy) * C36 * rho;
+        t[4] = (gx + gz) * C36 * rho;
+        t[5] = (gx - gz) * C36 * rho;
+        t[6] = (gz - gy) * C36 * rho;
+        t[7] = (gz + gy) * ((REAL)(-1.0f / 36.0f)) * rho;
+        t[8] = gz * C18 * rho;
+        return rho;
+    }
     REAL r = rho;
     r = gx * C18 * r; t[0] = r;
     r = gy * ((REAL)(-1.0f / 18.0f)) * r; t[1] = r;
@@ -383,7 +396,7 @@ void SFX(orc_init)(STOR *dd, int32_t *flags, REAL *vel, REAL *rho, const int32_t
 /* ------------------------------------------------------------------ alpha */
 void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_t nx, int64_t ny,
                     int64_t nz, REAL inv_tau, REAL gx, REAL gy, REAL gz, REAL lid, int store_vel,
-                    int store_rho, REAL tau0, REAL les_c) {
+                    int store_rho, REAL tau0, REAL les_c, int gmode) {
     grid_t g = mkgrid(nx, ny, nz, 0);
     const int64_t n = g.n;
 #pragma omp parallel for schedule(static)
@@ -400,7 +413,7 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
             if (fl == FL_FLUID) {
                 REAL A = dev_dp1(vx, vy, vz, dl);
                 dev_collide(g, dl, vx, vy, vz, m2, A, inv_tau, tau0, les_c);
-                r = gravity_chain(r, gx, gy, gz, t);
+                r = gravity_chain(r, gx, gy, gz, t, gmode);
                 write = 1;
             } else if (fl == FL_OBSTACLE) {
                 vx = 0; vy = 0; vz = 0;
@@ -408,7 +421,7 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
                 vx = lid; vy = 0; vz = 0;
                 REAL A = -K15 * (vx * vx);
                 dev_equilibria(vx, vy, vz, A, g);
-                r = gravity_chain((REAL)1.0f, gx, gy, gz, t);
+                r = gravity_chain((REAL)1.0f, gx, gy, gz, t, gmode);
                 write = 1;
             }
             if (write) {
@@ -453,7 +466,7 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
             REAL v2 = (vx * vx + vy * vy) + vz * vz;
             REAL dp = r - K15 * v2;
             collide(f, r, vx, vy, vz, dp, inv_tau, tau0, les_c);
-            r = gravity_chain(r, gx, gy, gz, t);
+            r = gravity_chain(r, gx, gy, gz, t, gmode);
             write = 1;
         } else if (fl == FL_OBSTACLE) {
             vx = 0; vy = 0; vz = 0; /* lbm_alpha.cl:338-342, no population write */
@@ -463,7 +476,7 @@ void SFX(orc_alpha)(STOR *dd, const int32_t *flags, REAL *vel, REAL *rho, int64_
             REAL v2 = (vx * vx + vy * vy) + vz * vz;
             REAL dp = r - K15 * v2;
             equilibria(vx, vy, vz, dp, f);
-            r = gravity_chain(r, gx, gy, gz, t);
+            r = gravity_chain(r, gx, gy, gz, t, gmode);
             write = 1;
         }
         if (write) {

@@ -104,7 +104,7 @@ class OracleKernels:
         self._init = getattr(L, f"orc_init_{storage}")
         self._init.argtypes = [vp, vp, vp, vp, vp, i64, i64, i64]
         self._alpha = getattr(L, f"orc_alpha_{storage}")
-        self._alpha.argtypes = [vp, vp, vp, vp, i64, i64, i64, R, R, R, R, R, ci, ci, R, R]
+        self._alpha.argtypes = [vp, vp, vp, vp, i64, i64, i64, R, R, R, R, R, ci, ci, R, R, ci]
         self._beta = getattr(L, f"orc_beta_{storage}")
         self._beta.argtypes = [vp, vp, vp, vp, i64, i64, i64, R, R, R, R, R, ci, ci, R, R, i64]
         self._perturb = getattr(L, f"orc_perturb_{storage}")
@@ -120,7 +120,8 @@ class OracleKernels:
 
     def alpha(self, lat: "Lattice", p: "Params"):
         self._alpha(_ptr(lat.dd), _ptr(lat.flags), _ptr(lat.vel), _ptr(lat.rho), *lat.dims,
-                    p.inv_tau, *p.gravity, p.lid, int(p.store_vel), int(p.store_rho), p.tau0, p.les_c)
+                    p.inv_tau, *p.gravity, p.lid, int(p.store_vel), int(p.store_rho), p.tau0, p.les_c,
+                    int(p.gravity_mode))
 
     def beta(self, lat: "Lattice", p: "Params"):
         self._beta(_ptr(lat.dd), _ptr(lat.flags), _ptr(lat.vel), _ptr(lat.rho), *lat.dims,
@@ -190,6 +191,8 @@ class RefKernels:
         self._check(lat)
         if p.les_c != 0:
             raise ValueError("the reference has no subgrid model")
+        if p.gravity_mode:
+            raise ValueError("the reference has only its own (aliased) gravity terms")
         self._alpha(_ptr(lat.dd), _ptr(lat.flags), _ptr(lat.vel), _ptr(lat.rho), p.inv_tau, *p.gravity, p.lid)
 
     def beta(self, lat, p):
@@ -207,7 +210,8 @@ class Params:
 
     les_c = 18*sqrt(2)*Cs^2 (0 turns the model off) and tau0 = 1/inv_tau is
     the molecular relaxation time.  wg selects the reference beta kernel's
-    work-group realignment semantics in the C oracle (0 = plain linear wrap)."""
+    work-group realignment semantics in the C oracle (0 = plain linear wrap).
+    gravity_mode 1 is the optional per-term forcing (not the reference's)."""
 
     inv_tau: float
     tau0: float = 0.0
@@ -217,6 +221,7 @@ class Params:
     store_vel: bool = True
     store_rho: bool = True
     wg: int = 0
+    gravity_mode: int = 0
 
     @staticmethod
     def lattice(tau: float, lid: float, cs: float = 0.0, dtype=np.float32, **kw) -> "Params":

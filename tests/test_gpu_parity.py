@@ -19,7 +19,7 @@ TOL = {"f32": 1e-6, "f64": 1e-12, "f16": 1e-6, "bf16": 1e-6}
 
 
 def gpu_params(api, p):
-    return api.Params.make(p.inv_tau, p.tau0, p.les_c, p.gravity, p.lid)
+    return api.Params.make(p.inv_tau, p.tau0, p.les_c, p.gravity, p.lid, p.gravity_mode)
 
 
 def gpu_single(api, O, dims, storage, p, lid=True, perturb=None, bc=None):
@@ -50,10 +50,10 @@ def compare(api, O, L, sol, storage, where=""):
     assert n_diff(rho, sol.lat.rho) == 0, f"density {where}"
 
 
-def oracle_params(O, storage, dims, cs=0.0, gravity=(0.0, 0.0, 0.0), re=300.0, u=0.05):
+def oracle_params(O, storage, dims, cs=0.0, gravity=(0.0, 0.0, 0.0), re=300.0, u=0.05, gravity_mode=0):
     rdt = O.STORAGE[storage][1]
     return O.Params.lattice(O.cavity_tau(u, dims[0], re), u, cs, dtype=rdt,
-                            gravity=tuple(float(rdt(g)) for g in gravity))
+                            gravity=tuple(float(rdt(g)) for g in gravity), gravity_mode=gravity_mode)
 
 
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
@@ -69,16 +69,18 @@ def test_init_matches_oracle(capi, oracle_mod, storage):
 
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
 @pytest.mark.parametrize("cs", [0.0, 0.17])
-@pytest.mark.parametrize("gravity", [(0.0, 0.0, 0.0), (1e-5, -2e-5, 3e-6)])
+@pytest.mark.parametrize("gravity,gmode", [((0.0, 0.0, 0.0), 0), ((1e-5, -2e-5, 3e-6), 0),
+                                           ((1e-5, -2e-5, 3e-6), 1)])
 @pytest.mark.parametrize("dims,shape", [((21, 14, 11), 1), ((22, 14, 11), 2), ((64, 12, 18), 2),
                                         ((21, 14, 11), 3), ((64, 12, 18), 3)])
-def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity, dims, shape):
+def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity, gmode, dims, shape):
     """Perturbed lid cavity: every array, every step, for the one-cell, the
     two-cell (needs an even x extent; the 64-wide case has whole warps inside
     the lattice) and the staged-tile kernel shapes (the 64x12x18 case spans
-    many tiles and ends in a partial one)."""
+    many tiles and ends in a partial one), with the reference's gravity terms
+    and with the optional per-term forcing."""
     api, O = capi, oracle_mod
-    p = oracle_params(O, storage, dims, cs, gravity)
+    p = oracle_params(O, storage, dims, cs, gravity, gravity_mode=gmode)
     L = gpu_single(api, O, dims, storage, p, perturb=(SEED, 2e-2))
     L.set_kernel_shape(shape)
     s = O.single(O.OracleKernels(storage), dims, p, storage)

@@ -322,3 +322,39 @@ def test_encode_decode_roundtrip(oracle_mod):
         g = k.decode(k.encode(f))
         tol = {"f32": 0, "f64": 0, "f16": 1e-3, "bf16": 1e-2}[st]
         assert np.max(np.abs(g - f)) <= tol * 0.4 + 1e-12
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_per_term_gravity_forcing(oracle_mod, storage):
+    """The optional forcing (gravity_mode 1): after one alpha step the change
+    against a zero-gravity step is, per opposite pair, +-(coefficient x
+    density), and the stored density is the population sum; the default
+    mode keeps the reference's chained terms (stored density = last term)."""
+    O = oracle_mod
+    rdt = O.STORAGE[storage][1]
+    dims = (9, 8, 7)
+    g = (rdt(2e-4), rdt(-3e-4), rdt(1e-4))
+    out = {}
+    for mode, grav in ((1, g), (1, (0.0, 0.0, 0.0)), (0, g)):
+        p = O.Params.lattice(0.6, 0.0, dtype=rdt, gravity=tuple(float(v) for v in grav), gravity_mode=mode)
+        s = O.Solver(O.OracleKernels(storage), dims, [O.FLAG_OBSTACLE] * 6, p, storage)
+        s.k.perturb(s.lat, (0, 0, 0), dims, 5, 2e-2)
+        rho_in = s.lat.dd.astype(np.float64).sum(0)
+        s.lat.counter = 1  # the next step is alpha
+        s.step()
+        out[(mode, grav == g)] = (s.lat.dd.astype(np.float64), s.lat.rho.astype(np.float64), rho_in)
+    m = s.lat.flags == O.FLAG_FLUID
+    f_g, rho_g, rho_in = out[(1, True)]
+    f_0, _, _ = out[(1, False)]
+    gx, gy, gz = (float(v) for v in g)
+    w18, w36 = float(np.float32(1 / 18)), float(np.float32(1 / 36))
+    coef = [gx * w18, -gy * w18, (gx - gy) * w36, (gx + gy) * w36, (gx + gz) * w36, (gx - gz) * w36,
+            (gz - gy) * w36, -(gz + gy) * w36, gz * w18]
+    tol = 1e-12 if storage == "f64" else 2e-7
+    for k, c in enumerate(coef):
+        # alpha writes f_2k into slot 2k+1 and f_2k+1 into slot 2k
+        np.testing.assert_allclose((f_g - f_0)[2 * k + 1][m], c * rho_in[m], rtol=1e-5, atol=tol)
+        np.testing.assert_allclose((f_g - f_0)[2 * k][m], -c * rho_in[m], rtol=1e-5, atol=tol)
+    np.testing.assert_allclose(rho_g[m], rho_in[m], rtol=1e-6)
+    _, rho_ref, _ = out[(0, True)]
+    assert np.abs(rho_ref[m]).max() < 1e-20  # the reference's chain: the product of nine small terms

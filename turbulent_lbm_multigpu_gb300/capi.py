@@ -43,12 +43,13 @@ class Params(C.Structure):
     """lbm_params: kernel arguments in double (rounded to the arithmetic type by the library)."""
 
     _fields_ = [("inv_tau", C.c_double), ("tau0", C.c_double), ("les_c", C.c_double),
-                ("gravity", C.c_double * 3), ("lid", C.c_double)]
+                ("gravity", C.c_double * 3), ("lid", C.c_double), ("gravity_mode", C.c_int32)]
 
     @staticmethod
-    def make(inv_tau: float, tau0: float = 0.0, les_c: float = 0.0, gravity=(0.0, 0.0, 0.0), lid: float = 0.0):
+    def make(inv_tau: float, tau0: float = 0.0, les_c: float = 0.0, gravity=(0.0, 0.0, 0.0), lid: float = 0.0,
+             gravity_mode: int = 0):
         p = Params()
-        p.inv_tau, p.tau0, p.les_c, p.lid = inv_tau, tau0, les_c, lid
+        p.inv_tau, p.tau0, p.les_c, p.lid, p.gravity_mode = inv_tau, tau0, les_c, lid, gravity_mode
         for a in range(3):
             p.gravity[a] = gravity[a]
         return p

@@ -83,6 +83,7 @@ void set_params_desc(LatDesc &h, int storage, const lbm_params &p) {
         for (int i = 0; i < 16; i++) h.pd[i] = (double)h.pf[i];
     }
     h.grav = grav;
+    h.gmode = p.gravity_mode ? 1 : 0;
 }
 
 // ---------------------------------------------------------------- kernels

@@ -211,7 +211,8 @@ struct LatDesc {
     int32_t nx, ny, nz;
     int32_t first_block;  // first block of this lattice in a batched launch
     int32_t nblocks;      // blocks of the launched kernel shape
-    int32_t grav;         // gravity chain non-zero (alpha kernel)
+    int32_t grav;         // gravity terms non-zero (alpha kernel)
+    int32_t gmode;        // 0: the reference's chained terms, 1: per-term forcing
     int32_t parity;       // step counter parity at the start of a batch tick
     double pd[16];        // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
     float pf[16];
@@ -335,9 +336,15 @@ __device__ __forceinline__ void collide(M f[19], M rho, M vx, M vy, M vz, M dp, 
 // Gravity terms of the alpha kernel.  The reference aliases its temporary to
 // rho (lbm_alpha.cl:173): term k is coefficient k times term k-1, and the
 // stored density is the last term.  Coefficients k0..k8 come pre-multiplied
-// from the host.
+// from the host.  gmode 1 (off by default) computes what the reference
+// intends instead: term k = coefficient k times the density.
 template <typename M>
 __device__ __forceinline__ M gravity_chain(M rho, const LatDesc &d, M t[9]) {
+    if (d.gmode) {  // per-term forcing: coefficient k times the density, density stored as is
+#pragma unroll
+        for (int k = 0; k < 9; k++) t[k] = parm<M>(d, P_K0 + k) * rho;
+        return rho;
+    }
     M r = rho;
 #pragma unroll
     for (int k = 0; k < 9; k++) {
