@@ -460,18 +460,24 @@ static int sm_count() {
     return cache[dev];
 }
 
-template <typename S, bool LES, bool BETA>
-static int launch_staged_k(const DomainArgs &a, int tiles, cudaStream_t st) {
+template <typename S, bool LES, bool BETA, bool ONE>
+static int launch_staged_one(const DomainArgs &a, int tiles, cudaStream_t st) {
     static bool attr = false;  // the ring exceeds the default 48 KB of dynamic shared memory
     if (!attr) {
-        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 Tile<S>::SMEM));
         attr = true;
     }
     const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
-    k_step_staged<S, LES, BETA><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
+    k_step_staged<S, LES, BETA, ONE><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
     CU(cudaGetLastError());
     return 0;
+}
+
+template <typename S, bool LES, bool BETA>
+static int launch_staged_k(const DomainArgs &a, int tiles, cudaStream_t st) {
+    return a.ntab == 1 ? launch_staged_one<S, LES, BETA, true>(a, tiles, st)
+                       : launch_staged_one<S, LES, BETA, false>(a, tiles, st);
 }
 
 template <typename S>

