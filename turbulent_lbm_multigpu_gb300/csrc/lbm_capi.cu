@@ -498,12 +498,12 @@ static int staged_cells(int storage) {
 
 int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
                 cudaStream_t st) {
-    // the staged beta needs rows of whole 128-byte lines (nx a multiple of 32
-    // float or 64 half populations)
+    // the staged beta needs rows of whole 16-byte units (nx a multiple of 4
+    // float or 8 half populations)
     bool staged = shape == 3 && storage != kF64;
     if (staged && parity == 0)
         for (int i = 0; i < ntab; i++)
-            if ((htab[i].nx * storage_bytes(storage)) % 128) staged = false;
+            if ((htab[i].nx * storage_bytes(storage)) % 16) staged = false;
     const bool pair = shape == 2;
     const int per = staged ? staged_cells(storage) : cells_per_block(pair);
     for (int c0 = 0; c0 < ntab; c0 += kParamLattices) {

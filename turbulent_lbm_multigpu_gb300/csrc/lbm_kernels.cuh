@@ -60,8 +60,12 @@ __host__ __device__ constexpr int opp(int i) { return i == 18 ? 18 : (i ^ 1); }
 // Two float lanes (two cells).  Every lane is one IEEE round-to-nearest
 // operation (__fadd_rn/__fsub_rn/__fmul_rn are never contracted into a
 // multiply-add), so a pair computes exactly what two scalar cells compute.
-// The packed f32x2 PTX forms were measured to differ from the scalar result
-// by up to 5 ulp in this kernel, so they are not used.
+// Blackwell's packed FP32x2 instructions (add/sub/mul/fma.rn.f32x2) are
+// exact per lane when used alone (measured on GB300 against the scalar
+// intrinsics over 2^20 random operands, subnormals included), but the
+// assembler may fuse a packed multiply into a following packed add: the
+// collision with packed arithmetic differed from the scalar one by up to
+// 4 ulp in 1.4 % of the values.  So the lanes stay scalar.
 struct P2 {
     float x, y;
 };
@@ -936,8 +940,8 @@ __global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ Domai
 //          go back into the segments (slot opp(i)) and the producer writes
 //          the tile back with bulk stores.
 //   beta:  segment i holds the tile's sources of f_i, plane opp(i) at
-//          c - e_i, from the 128-byte line below (T + A elements; nx is a
-//          multiple of A, so the offset into the segment is fixed per
+//          c - e_i, from the 16-byte boundary below (T + A elements; nx is
+//          a multiple of A, so the offset into the segment is fixed per
 //          direction); the results scatter to c + e_i with ordinary
 //          stores.  Tiles within reach of either end of the buffer (their
 //          sources wrap) and a partial last tile take the one-cell path
@@ -956,7 +960,7 @@ __device__ unsigned int g_stage_error;
 template <typename S> struct Tile {
     static_assert(sizeof(S) <= 4, "staged tiles hold float, half or bfloat16 populations");
     static constexpr int T = 1024 / (int)sizeof(S);  // cells per tile: 1 KB per plane
-    static constexpr int A = 128 / (int)sizeof(S);   // elements per 128-byte line
+    static constexpr int A = 16 / (int)sizeof(S);    // elements per 16-byte boundary
     static constexpr int PER = (T + 32 * kConsumerWarps - 1) / (32 * kConsumerWarps);  // cells per compute thread
     static constexpr int SEG = (T + A) * (int)sizeof(S);   // bytes per plane segment
     static constexpr int STAGE = 19 * SEG + T;       // 19 segments + flag bytes
