@@ -131,6 +131,7 @@ template <> struct Store<__half> {
         return P2{v.x, v.y};
     }
     __device__ static __forceinline__ void dst2(__half *p, P2 v) { *(__half2 *)p = __floats2half2_rn(v.x, v.y); }
+    __device__ static __forceinline__ uint32_t dbits(R v) { return __half_as_ushort(__float2half_rn(v)); }
     __device__ static __forceinline__ R ld(const __half *p, R w) { return __half2float(*p) + w; }
     __device__ static __forceinline__ void st(__half *p, R v, R w) { *p = __float2half_rn(v - w); }
     __device__ static __forceinline__ P2 ld2(const __half *p, R w) {
@@ -154,6 +155,7 @@ template <> struct Store<__nv_bfloat16> {
     __device__ static __forceinline__ void dst2(__nv_bfloat16 *p, P2 v) {
         *(__nv_bfloat162 *)p = __floats2bfloat162_rn(v.x, v.y);
     }
+    __device__ static __forceinline__ uint32_t dbits(R v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
     __device__ static __forceinline__ R ld(const __nv_bfloat16 *p, R w) { return __bfloat162float(*p) + w; }
     __device__ static __forceinline__ void st(__nv_bfloat16 *p, R v, R w) { *p = __float2bfloat16_rn(v - w); }
     __device__ static __forceinline__ P2 ld2(const __nv_bfloat16 *p, R w) {
@@ -1114,6 +1116,59 @@ __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigne
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
+// Two neighbouring cells l, l + 1 (l and c even) of an inside beta tile in
+// 16-bit storage.  The ten populations with an x component scatter one by
+// one; the nine without one land at the same in-row offset for both cells,
+// a 4-byte aligned pair (c, nx and the plane stride are even), and go out
+// as one 32-bit store after the second cell, the first cell's halves held
+// two to a register meanwhile.  Used with the subgrid model (measured at
+// 512^3: f16 70.1k -> 73.6k MLUPS); without it the held halves push the
+// register-capped kernel into spills and the one-cell loop stays faster.
+template <typename S, bool LES>
+__device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
+                                                 int store_v, int store_rho) {
+    using TL = Tile<S>;
+    using R = typename Store<S>::R;
+    static_assert(Store<S>::kDev, "pairs of 16-bit populations");
+    const int64_t nx = d.nx, sl = (int64_t)d.nx * d.ny, ps = d.pstride;
+    S *const pc = (S *)d.dd + c;
+    uint32_t keep[5];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int fl = stage[19 * TL::SEG + l + h];
+        R f[19];
+#pragma unroll
+        for (int i = 0; i < 19; i++) {
+            const int rem = (-dir_x(i)) & (TL::A - 1);
+            f[i] = pop_ld<S>((const S *)(stage + i * TL::SEG) + (l + h + rem), i);
+        }
+        R r, vx, vy, vz;
+        beta_phys<R, LES, true>(fl, f, r, vx, vy, vz, d);
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < 19; i++) {
+            if (dir_x(i) != 0) {
+                pop_st<S>(pc + (h + i * ps + dir_off(i, nx, sl)), f[i], i);
+                continue;
+            }
+            const uint32_t bits = Store<S>::dbits(f[i]);
+            if (h == 0) {
+                keep[k >> 1] = (k & 1) ? (keep[k >> 1] | (bits << 16)) : bits;
+            } else {
+                const uint32_t first = (k & 1) ? (keep[k >> 1] >> 16) : (keep[k >> 1] & 0xffffu);
+                *(uint32_t *)(pc + (i * ps + dir_off(i, nx, sl))) = first | (bits << 16);
+            }
+            k++;
+        }
+        if (fl == kGhost) continue;  // lbm_beta.cl:787-788
+        if (store_v) {
+            R *u = (R *)d.vel + c + h;
+            u[0] = vx; u[d.n] = vy; u[2 * d.n] = vz;
+        }
+        if (store_rho) ((R *)d.rho)[c + h] = r;
+    }
+}
+
 template <typename S, bool LES>
 __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned char *stage, int l, int64_t c,
                                                   int store_v, int store_rho) {
@@ -1191,6 +1246,10 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
                 const int64_t c = c0 + l;
                 if (l < TL::T && c < d.n) beta_cell<S, LES, true>(d, c, a.store_v, a.store_rho);
             }
+        } else if constexpr (BETA && LES && Store<S>::kDev) {
+#pragma unroll 1
+            for (int l = 2 * threadIdx.x; l < TL::T; l += 64 * kConsumerWarps)
+                beta_staged_pair<S, LES>(d, stage, l, c0 + l, a.store_v, a.store_rho);
         } else {
 #pragma unroll 1
             for (int m = 0; m < TL::PER; m++) {
