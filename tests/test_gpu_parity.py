@@ -176,12 +176,15 @@ def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph, sha
         assert got == ref[done - 1], f"step {done}"
 
 
-@pytest.mark.parametrize("storage,nums,halo_mode", [("f32", (2, 2, 1), 0), ("f64", (2, 2, 1), 0),
-                                                    ("f16", (2, 2, 1), 0), ("f32", (3, 2, 2), 1),
-                                                    ("bf16", (2, 1, 3), 1)])
-def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, nums, halo_mode):
+@pytest.mark.parametrize("storage,size,nums,halo_mode", [
+    ("f32", (30, 20, 12), (2, 2, 1), 0), ("f64", (30, 20, 12), (2, 2, 1), 0),
+    ("f16", (30, 20, 12), (2, 2, 1), 0), ("f32", (36, 24, 24), (3, 2, 2), 1),
+    ("bf16", (36, 24, 24), (2, 1, 3), 1),
+    # subdomains 32 and 16 cells wide: the staged beta tiles (two cells per
+    # thread with the subgrid model) run over ghost layers
+    ("f16", (64, 24, 20), (2, 2, 1), 1), ("bf16", (48, 16, 24), (3, 1, 2), 0)])
+def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, size, nums, halo_mode):
     api, O = capi, oracle_mod
-    size = (30, 20, 12) if nums == (2, 2, 1) else (36, 24, 24)
     p = oracle_params(O, storage, (28, 0, 0), cs=0.17, re=5000.0, u=0.1)
     D = api.Domain(size, nums, api.STORAGE_NAMES[storage], True, True)
     D.set_params(gpu_params(api, p))
