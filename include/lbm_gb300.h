@@ -271,9 +271,13 @@ int lbm_cu_run(lbm_lattice *lat, int64_t first_step, int64_t steps, void *stream
 int lbm_cu_batch_create(const lbm_cavity *cavities, int count, int store_velocity, lbm_batch **out);
 int lbm_cu_batch_destroy(lbm_batch *b);
 int lbm_cu_batch_reset(lbm_batch *b, void *stream);
+/* Ensemble kernel shape: 1 one cell per thread (default), 2 two cells per
+ * thread (cavities with even nx), 3 as 1 but the alpha steps of half and
+ * bfloat16 cavities run the staged tiles when every member of a launch is
+ * at an alpha step.  Results are the same for every shape. */
 int lbm_cu_batch_set_kernel_shape(lbm_batch *b, int cells_per_thread);
 /* Autotuner: times `trial_steps` steps of the whole ensemble for each kernel
- * shape (one or two cells per thread), keeps the fastest, and resets. */
+ * shape (1, 2, 3), keeps the fastest, and resets. */
 int lbm_cu_batch_tune(lbm_batch *b, int trial_steps, int *cells_per_thread, double *ms_per_step, void *stream);
 /* Run until every cavity has taken its steps, or at most max_steps steps
  * (max_steps < 0: no limit). */
@@ -289,6 +293,7 @@ lbm_lattice *lbm_cu_batch_lattice(lbm_batch *b, int index);
  * until released.  A solve's result does not depend on what else runs. */
 int lbm_cu_server_create(double hbm_budget_bytes, int max_active, int store_velocity, lbm_server **out);
 int lbm_cu_server_destroy(lbm_server *s);
+/* As lbm_cu_batch_set_kernel_shape; a server starts with shape 3. */
 int lbm_cu_server_set_kernel_shape(lbm_server *s, int cells_per_thread);
 int lbm_cu_server_submit(lbm_server *s, const lbm_cavity *c, int64_t *id);
 int lbm_cu_server_tick(lbm_server *s, int64_t max_steps, int use_graph, int *admitted, void *stream);

@@ -38,7 +38,7 @@ def mix(api):
             C((10, 30, 12), api.F32, 0.58, 0.17, 0.05, 11, 19, 1e-2)]
 
 
-@pytest.mark.parametrize("shape,use_graph", [(1, True), (2, True), (1, False)])
+@pytest.mark.parametrize("shape,use_graph", [(1, True), (2, True), (1, False), (3, True), (3, False)])
 def test_batch_matches_lone_cavities(capi, shape, use_graph):
     api = capi
     cav = mix(api)
@@ -59,7 +59,7 @@ def test_batch_autotuner_keeps_results(capi):
     cav = mix(api)
     B = api.Batch(cav, store_velocity=True)
     shape, ms = B.tune(trial_steps=6)
-    assert shape in (1, 2) and ms > 0
+    assert shape in (1, 2, 3) and ms > 0
     B.run()
     for c, L in zip(cav, B.lattices):
         assert n_diff(L.read(api.FIELD_DD), lone(api, c).read(api.FIELD_DD)) == 0
@@ -80,12 +80,16 @@ def test_batch_partial_runs_add_up(capi):
         assert n_diff(La.read(api.FIELD_DD), Lb.read(api.FIELD_DD)) == 0
 
 
-def test_server_results_do_not_depend_on_the_mix(capi):
+@pytest.mark.parametrize("shape", [1, 3])
+def test_server_results_do_not_depend_on_the_mix(capi, shape):
     """Solves admitted at different ticks, sharing launches with different
-    neighbours, finish with the fields they have when run alone."""
+    neighbours, finish with the fields they have when run alone (shape 3:
+    launches whose 16-bit members are all at an alpha step run the staged
+    tiles, the others the one-cell kernel)."""
     api = capi
     cav = mix(api)
     S = api.Server(hbm_budget_bytes=64 << 20)
+    S.set_kernel_shape(shape)
     ids = []
     finished = {}
     for k, c in enumerate(cav):

@@ -5,7 +5,9 @@
 // counter.  A tick advances every active cavity by k steps with one launch
 // per storage group and step (k_step / k_step2: each block reads its
 // cavity's parity from the descriptor table), pairs of steps replayed from a
-// captured CUDA graph.  The static batch (lbm_cu_batch_*) runs a fixed
+// captured CUDA graph.  With kernel shape 3 a chunk of 16-bit cavities whose
+// members are all at an alpha step runs the staged-tile kernel instead (the
+// staged beta needs aligned rows and one parity per launch).  The static batch (lbm_cu_batch_*) runs a fixed
 // ensemble to completion; the server (lbm_cu_server_*) admits queued solves
 // between ticks under an HBM budget and retires finished ones (continuous
 // batching).  Results of a cavity do not depend on the other members of its
@@ -119,12 +121,16 @@ struct Ensemble {
     // One launch per chunk of up to kBatchLattices members per step.
     struct Chunk {
         std::unique_ptr<BatchArgs> args;  // descriptors with this tick's parities
+        std::unique_ptr<BatchArgs> sargs;  // the same numbered in staged tiles (staged groups)
         int blocks = 0;
+        int tiles = 0;
+        int parities = 0;  // bit p: some member's step counter has parity p
         bool les = false;
     };
     struct Group {
         int storage = 0;
         bool pair = false;
+        bool staged = false;  // alpha steps through the staged tiles (shape 3, 16-bit storage)
         std::vector<int> members;
         std::vector<Chunk> chunks;
         int32_t *dmap = nullptr;  // lattice index (within its chunk) of every block
@@ -171,6 +177,7 @@ struct Ensemble {
                 g = &groups.back();
                 g->storage = s.spec.storage;
                 g->pair = pair;
+                g->staged = shape == 3 && (s.spec.storage == LBM_F16 || s.spec.storage == LBM_BF16);
             }
             g->members.push_back((int)i);
         }
@@ -184,7 +191,10 @@ struct Ensemble {
             CU(cudaMalloc((void **)&g.dmap, map.size() * sizeof(int32_t)));
             CU(cudaMemcpy(g.dmap, map.data(), map.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
             g.chunks.resize((g.members.size() + kBatchLattices - 1) / kBatchLattices);
-            for (auto &c : g.chunks) c.args.reset(new BatchArgs());
+            for (auto &c : g.chunks) {
+                c.args.reset(new BatchArgs());
+                if (g.staged) c.sargs.reset(new BatchArgs());
+            }
         }
         dirty = false;
         drop_graph();
@@ -204,8 +214,11 @@ struct Ensemble {
                 BatchArgs &a = *ch.args;
                 memset(&a, 0, sizeof(a));
                 const size_t k0 = c * kBatchLattices, k1 = std::min(g.members.size(), k0 + kBatchLattices);
-                int first = 0;
+                int first = 0, tile = 0;
+                const int tcells = g.staged ? staged_cells(g.storage) : 0;
+                if (g.staged) memset(ch.sargs.get(), 0, sizeof(BatchArgs));
                 ch.les = false;
+                ch.parities = 0;
                 for (size_t k = k0; k < k1; k++) {
                     const Slot &s = slots[g.members[k]];
                     LatDesc h = s.lat->h;
@@ -216,11 +229,20 @@ struct Ensemble {
                     if (uses_les(h)) ch.les = true;
                     a.tab[k - k0] = h;
                     parity.push_back(h.parity);
+                    ch.parities |= 1 << h.parity;
+                    if (g.staged) {
+                        h.first_block = tile;
+                        h.nblocks = (int)((h.n + tcells - 1) / tcells);
+                        tile += h.nblocks;
+                        ch.sargs->tab[k - k0] = h;
+                    }
                 }
                 a.ntab = (int)(k1 - k0);
                 a.block_lattice = g.dmap + map_off;
                 ch.blocks = first;
                 map_off += first;
+                if (g.staged) ch.sargs->ntab = a.ntab;
+                ch.tiles = tile;
             }
         }
         if (parity != graph_parity) drop_graph();
@@ -231,6 +253,13 @@ struct Ensemble {
     int launch_all(int j, bool store, cudaStream_t st) {
         for (auto &g : groups)
             for (auto &ch : g.chunks) {
+                if (g.staged && ch.parities == 1 << ((j + 1) & 1)) {
+                    // every member is at an alpha step: staged tiles
+                    ch.sargs->store_v = store ? store_v : 0;
+                    ch.sargs->store_rho = 0;
+                    if (launch_staged_alpha_batch(g.storage, ch.les, *ch.sargs, ch.tiles, st)) return -1;
+                    continue;
+                }
                 ch.args->store_v = store ? store_v : 0;
                 ch.args->store_rho = 0;
                 if (launch_tick(g.storage, g.pair, ch.les, *ch.args, ch.blocks, j, st)) return -1;
@@ -388,7 +417,7 @@ int lbm_cu_batch_reset(lbm_batch *b, void *stream) {
 
 int lbm_cu_batch_set_kernel_shape(lbm_batch *b, int cells_per_thread) {
     if (!b) return fail("NULL batch");
-    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
+    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("the ensemble kernel shape is 1, 2 or 3");
     b->e.shape = cells_per_thread;
     b->e.dirty = true;
     return 0;
@@ -416,7 +445,7 @@ int lbm_cu_batch_tune(lbm_batch *b, int trial_steps, int *cells_per_thread, doub
     CU(cudaEventCreate(&e1));
     double best_ms = 1e300;
     int best = 1;
-    for (int shape = 1; shape <= 2; shape++) {
+    for (int shape = 1; shape <= 3; shape++) {
         b->e.shape = shape;
         b->e.dirty = true;
         if (lbm_cu_batch_reset(b, stream)) return -1;
@@ -470,6 +499,7 @@ int lbm_cu_server_create(double hbm_budget_bytes, int max_active, int store_velo
     s->budget = hbm_budget_bytes;
     s->max_active = max_active > 0 ? max_active : 1 << 30;
     s->e.store_v = store_velocity ? 1 : 0;
+    s->e.shape = 3;  // staged alpha steps for parity-uniform 16-bit launches (measured the faster)
     *out = s;
     return 0;
 }
@@ -481,7 +511,7 @@ int lbm_cu_server_destroy(lbm_server *s) {
 
 int lbm_cu_server_set_kernel_shape(lbm_server *s, int cells_per_thread) {
     if (!s) return fail("NULL server");
-    if (cells_per_thread != 1 && cells_per_thread != 2) return fail("cells per thread is 1 or 2");
+    if (cells_per_thread < 1 || cells_per_thread > 3) return fail("the ensemble kernel shape is 1, 2 or 3");
     s->e.shape = cells_per_thread;
     s->e.dirty = true;
     return 0;

@@ -460,16 +460,16 @@ static int sm_count() {
     return cache[dev];
 }
 
-template <typename S, bool LES, bool BETA, bool ONE>
-static int launch_staged_one(const DomainArgs &a, int tiles, cudaStream_t st) {
+template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
+static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     static bool attr = false;  // the ring exceeds the default 48 KB of dynamic shared memory
     if (!attr) {
-        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 Tile<S>::SMEM));
         attr = true;
     }
     const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
-    k_step_staged<S, LES, BETA, ONE><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
+    k_step_staged<S, LES, BETA, ONE, N><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
     CU(cudaGetLastError());
     return 0;
 }
@@ -487,13 +487,29 @@ static int launch_staged_t(int parity, bool les, const DomainArgs &a, int tiles,
     return les ? launch_staged_k<S, true, true>(a, tiles, st) : launch_staged_k<S, false, true>(a, tiles, st);
 }
 
-static int staged_cells(int storage) {
+int staged_cells(int storage) {
     switch (storage) {
         case kF32: return Tile<float>::T;
         case kF16: return Tile<__half>::T;
         case kBF16: return Tile<__nv_bfloat16>::T;
     }
     return 0;
+}
+
+template <typename S>
+static int launch_staged_alpha_batch_t(bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
+    if (tiles <= 0) return 0;
+    return les ? launch_staged_one<S, true, false, false, kBatchLattices>(a, tiles, st)
+               : launch_staged_one<S, false, false, false, kBatchLattices>(a, tiles, st);
+}
+
+int launch_staged_alpha_batch(int storage, bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
+    switch (storage) {
+        case kF32: return launch_staged_alpha_batch_t<float>(les, a, tiles, st);
+        case kF16: return launch_staged_alpha_batch_t<__half>(les, a, tiles, st);
+        case kBF16: return launch_staged_alpha_batch_t<__nv_bfloat16>(les, a, tiles, st);
+    }
+    return fail("the staged kernels take float, half or bfloat16 storage");
 }
 
 int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,

@@ -956,6 +956,9 @@ constexpr int kConsumerWarps = 8;
 constexpr int kStageThreads = 32 * (kConsumerWarps + 1);
 constexpr unsigned kStageTimeout = 1u;
 constexpr uint32_t kStageWaitLimit = 1u << 22;
+// Header of the dynamic shared memory: full/empty barriers from byte 0, the
+// tiles' descriptor indices from byte 64, the ring from byte 128.
+static_assert(2 * kStages * 8 <= 64 && 64 + 4 * kStages <= 128, "the ring header holds the barriers and indices");
 
 __device__ unsigned int g_stage_error;
 
@@ -1016,18 +1019,20 @@ __device__ __forceinline__ void fence_barrier_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Lattice of tile t (first_block / nblocks count tiles here).  ONE: the
-// launch covers a single lattice, whose descriptor fields are then read at
-// fixed parameter offsets (measured 4 % faster than the indexed reads).
+// Descriptor index of the lattice of tile t (first_block / nblocks count
+// tiles here).  ONE: the launch covers a single lattice, whose descriptor
+// fields are then read at fixed parameter offsets (measured 4 % faster than
+// the indexed reads).  The producer searches once per tile and leaves the
+// index beside the ring buffer for the compute warps.
 template <bool ONE, int N>
-__device__ __forceinline__ const LatDesc &lattice_of_unit(const StepArgs<N> &a, int t) {
-    if (ONE) return a.tab[0];
+__device__ __forceinline__ int lattice_index(const StepArgs<N> &a, int t) {
+    if (ONE) return 0;
     int li = 0, hi = a.ntab - 1;
     while (li < hi) {
         const int mid = (li + hi + 1) >> 1;
         if (a.tab[mid].first_block <= t) li = mid; else hi = mid - 1;
     }
-    return a.tab[li];
+    return li;
 }
 
 // A beta tile whose shifted segments lie inside the lattice: every source
@@ -1044,17 +1049,21 @@ __device__ __forceinline__ bool beta_tile_inside(const LatDesc &d, int64_t c0) {
 // address arithmetic over its lanes).  A beta tile that is not inside gets
 // no copies: its phase completes at once and the compute warps read it from
 // global memory.
-template <typename S, bool BETA, bool ONE>
-__device__ __forceinline__ void stage_tile(const DomainArgs &a, int t, unsigned char *stage, uint64_t *bar,
-                                           int lane) {
+template <typename S, bool BETA, bool ONE, int N>
+__device__ __forceinline__ void stage_tile(const StepArgs<N> &a, int t, unsigned char *stage, uint64_t *bar,
+                                           int *lat_slot, int lane) {
     using TL = Tile<S>;
-    const LatDesc &d = lattice_of_unit<ONE>(a, t);
+    const int li = lattice_index<ONE>(a, t);
+    const LatDesc &d = a.tab[li];
     const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
     const bool inside = !BETA || beta_tile_inside<S>(d, c0);
     const int cells = (int)min((int64_t)TL::T, d.n - c0);
     const uint32_t pb = BETA ? (uint32_t)TL::SEG : (uint32_t)((cells * (int)sizeof(S) + 15) & ~15);
     const uint32_t fb = BETA ? (uint32_t)TL::T : (uint32_t)((cells + 15) & ~15);
-    if (lane == 0) mbar_expect_tx(bar, inside ? 19 * pb + fb : 0);
+    if (lane == 0) {
+        *lat_slot = li;  // ordered before the arrival (release) that completes with the copies
+        mbar_expect_tx(bar, inside ? 19 * pb + fb : 0);
+    }
     __syncwarp();
     if (!inside) return;
     if (lane < 19) {
@@ -1072,11 +1081,12 @@ __device__ __forceinline__ void stage_tile(const DomainArgs &a, int t, unsigned 
 
 // Write an alpha tile back from its ring buffer, lane i < 19 plane i, and
 // wait until the buffer has been read out.
-template <typename S, bool ONE>
-__device__ __forceinline__ void unstage_tile(const DomainArgs &a, int t, const unsigned char *stage, int lane) {
+template <typename S, bool ONE, int N>
+__device__ __forceinline__ void unstage_tile(const StepArgs<N> &a, int t, int li, const unsigned char *stage,
+                                             int lane) {
     using TL = Tile<S>;
     if (lane < 19) {
-        const LatDesc &d = lattice_of_unit<ONE>(a, t);
+        const LatDesc &d = a.tab[ONE ? 0 : li];
         const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
         const int cells = (int)min((int64_t)TL::T, d.n - c0);
         const uint32_t pb = (uint32_t)((cells * (int)sizeof(S) + 15) & ~15);
@@ -1191,12 +1201,16 @@ __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned cha
     if (store_rho) ((R *)d.rho)[c] = r;
 }
 
-template <typename S, bool LES, bool BETA, bool ONE>
-__global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ DomainArgs a,
+// N: descriptors in the parameter space (kParamLattices for domains and
+// single lattices; kBatchLattices for the alpha steps of an ensemble chunk
+// whose members are all at an alpha step).
+template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
+__global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ StepArgs<N> a,
                                                                                   int tiles) {
     using TL = Tile<S>;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *full = (uint64_t *)smem, *empty = full + kStages;
+    int *tile_lat = (int *)(smem + 64);  // descriptor index of the tile in each buffer
     unsigned char *buf = smem + 128;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -1220,9 +1234,9 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
                 // the compute warps are done with the tile k - kStages in this buffer
                 ok = __all_sync(0xffffffffu, mbar_wait(&empty[s], (uint32_t)((k / kStages - 1) & 1)));
                 if (!ok) break;
-                if (!BETA) unstage_tile<S, ONE>(a, blockIdx.x + (k - kStages) * stride, stage, lane);
+                if (!BETA) unstage_tile<S, ONE, N>(a, blockIdx.x + (k - kStages) * stride, tile_lat[s], stage, lane);
             }
-            if (k < mine) stage_tile<S, BETA, ONE>(a, blockIdx.x + k * stride, stage, &full[s], lane);
+            if (k < mine) stage_tile<S, BETA, ONE, N>(a, blockIdx.x + k * stride, stage, &full[s], &tile_lat[s], lane);
         }
         if (!ok && lane == 0) atomicOr(&g_stage_error, kStageTimeout);
         bulk_wait_all();
@@ -1237,7 +1251,7 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
             break;
         }
         const int t = blockIdx.x + k * stride;
-        const LatDesc &d = lattice_of_unit<ONE>(a, t);
+        const LatDesc &d = a.tab[ONE ? 0 : tile_lat[s]];
         const int64_t c0 = (int64_t)(t - d.first_block) * TL::T;
         if (BETA && !beta_tile_inside<S>(d, c0)) {
 #pragma unroll 1
