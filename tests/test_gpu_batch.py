@@ -35,7 +35,10 @@ def mix(api):
             C((12, 12, 12), api.F32, 0.7, 0.0, 0.02, 0, 16, 0.0),
             C((26, 14, 22), api.F16, 0.51, 0.17, 0.09, 21, 17, 0.0),
             C((40, 24, 14), api.F32, 0.55, 0.17, 0.06, 25, 18, 1e-2),
-            C((10, 30, 12), api.F32, 0.58, 0.17, 0.05, 11, 19, 1e-2)]
+            C((10, 30, 12), api.F32, 0.58, 0.17, 0.05, 11, 19, 1e-2),
+            # rows of whole 16-byte units: with shape 3 their beta steps are staged too
+            C((32, 12, 14), api.F16, 0.54, 0.17, 0.06, 19, 20, 1e-2),
+            C((16, 20, 18), api.F16, 0.57, 0.17, 0.04, 15, 21, 1e-2)]
 
 
 @pytest.mark.parametrize("shape,use_graph", [(1, True), (2, True), (1, False), (3, True), (3, False)])

@@ -6,8 +6,9 @@
 // per storage group and step (k_step / k_step2: each block reads its
 // cavity's parity from the descriptor table), pairs of steps replayed from a
 // captured CUDA graph.  With kernel shape 3 a chunk of 16-bit cavities whose
-// members are all at an alpha step runs the staged-tile kernel instead (the
-// staged beta needs aligned rows and one parity per launch).  The static batch (lbm_cu_batch_*) runs a fixed
+// members are all at an alpha step runs the staged-tile kernel instead, and
+// so do beta steps of the cavities whose rows are whole 16-byte units (they
+// form their own groups).  The static batch (lbm_cu_batch_*) runs a fixed
 // ensemble to completion; the server (lbm_cu_server_*) admits queued solves
 // between ticks under an HBM budget and retires finished ones (continuous
 // batching).  Results of a cavity do not depend on the other members of its
@@ -131,6 +132,7 @@ struct Ensemble {
         int storage = 0;
         bool pair = false;
         bool staged = false;  // alpha steps through the staged tiles (shape 3, 16-bit storage)
+        bool aligned = false;  // staged, and every nx a multiple of 16 bytes: beta steps staged too
         std::vector<int> members;
         std::vector<Chunk> chunks;
         int32_t *dmap = nullptr;  // lattice index (within its chunk) of every block
@@ -169,15 +171,18 @@ struct Ensemble {
             const Slot &s = slots[i];
             if (!s.active) continue;
             const bool pair = shape == 2 && s.spec.storage != LBM_F64 && !(s.spec.nx & 1);
+            const bool staged = shape == 3 && (s.spec.storage == LBM_F16 || s.spec.storage == LBM_BF16);
+            const bool aligned = staged && ((int64_t)s.spec.nx * storage_bytes(s.spec.storage)) % 16 == 0;
             Group *g = nullptr;
             for (auto &x : groups)
-                if (x.storage == s.spec.storage && x.pair == pair) g = &x;
+                if (x.storage == s.spec.storage && x.pair == pair && x.aligned == aligned) g = &x;
             if (!g) {
                 groups.emplace_back();
                 g = &groups.back();
                 g->storage = s.spec.storage;
                 g->pair = pair;
-                g->staged = shape == 3 && (s.spec.storage == LBM_F16 || s.spec.storage == LBM_BF16);
+                g->staged = staged;
+                g->aligned = aligned;
             }
             g->members.push_back((int)i);
         }
@@ -253,11 +258,13 @@ struct Ensemble {
     int launch_all(int j, bool store, cudaStream_t st) {
         for (auto &g : groups)
             for (auto &ch : g.chunks) {
-                if (g.staged && ch.parities == 1 << ((j + 1) & 1)) {
-                    // every member is at an alpha step: staged tiles
+                const bool all_alpha = ch.parities == 1 << ((j + 1) & 1);
+                const bool all_beta = ch.parities == 1 << (j & 1);
+                if (g.staged && (all_alpha || (all_beta && g.aligned))) {
+                    // every member at the same kind of step: staged tiles
                     ch.sargs->store_v = store ? store_v : 0;
                     ch.sargs->store_rho = 0;
-                    if (launch_staged_alpha_batch(g.storage, ch.les, *ch.sargs, ch.tiles, st)) return -1;
+                    if (launch_staged_batch(g.storage, all_beta, ch.les, *ch.sargs, ch.tiles, st)) return -1;
                     continue;
                 }
                 ch.args->store_v = store ? store_v : 0;

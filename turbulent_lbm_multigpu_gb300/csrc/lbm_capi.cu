@@ -497,17 +497,20 @@ int staged_cells(int storage) {
 }
 
 template <typename S>
-static int launch_staged_alpha_batch_t(bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
+static int launch_staged_batch_t(bool beta, bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
     if (tiles <= 0) return 0;
+    if (beta)
+        return les ? launch_staged_one<S, true, true, false, kBatchLattices>(a, tiles, st)
+                   : launch_staged_one<S, false, true, false, kBatchLattices>(a, tiles, st);
     return les ? launch_staged_one<S, true, false, false, kBatchLattices>(a, tiles, st)
                : launch_staged_one<S, false, false, false, kBatchLattices>(a, tiles, st);
 }
 
-int launch_staged_alpha_batch(int storage, bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
+int launch_staged_batch(int storage, bool beta, bool les, const BatchArgs &a, int tiles, cudaStream_t st) {
     switch (storage) {
-        case kF32: return launch_staged_alpha_batch_t<float>(les, a, tiles, st);
-        case kF16: return launch_staged_alpha_batch_t<__half>(les, a, tiles, st);
-        case kBF16: return launch_staged_alpha_batch_t<__nv_bfloat16>(les, a, tiles, st);
+        case kF32: return launch_staged_batch_t<float>(beta, les, a, tiles, st);
+        case kF16: return launch_staged_batch_t<__half>(beta, les, a, tiles, st);
+        case kBF16: return launch_staged_batch_t<__nv_bfloat16>(beta, les, a, tiles, st);
     }
     return fail("the staged kernels take float, half or bfloat16 storage");
 }

@@ -53,9 +53,11 @@ int launch_step(int storage, int shape, int parity, bool les, const LatDesc *hta
                 cudaStream_t st);
 // Cells per staged tile of a storage type (0: not staged).
 int staged_cells(int storage);
-// An alpha step of up to kBatchLattices lattices through the staged tiles
-// (first_block / nblocks of the descriptors count tiles of staged_cells).
-int launch_staged_alpha_batch(int storage, bool les, const BatchArgs &a, int tiles, cudaStream_t st);
+// One step of up to kBatchLattices lattices, all at an alpha step or all at
+// a beta step, through the staged tiles (first_block / nblocks of the
+// descriptors count tiles of staged_cells; a beta step needs every nx a
+// multiple of 16 bytes of populations).
+int launch_staged_batch(int storage, bool beta, bool les, const BatchArgs &a, int tiles, cudaStream_t st);
 // One lattice block of a checkpoint file (lbm_io.cu).
 int ckpt_write_lattice(FILE *f, lbm_lattice *l, int64_t counter);
 int ckpt_read_lattice(FILE *f, lbm_lattice *l, int64_t *counter);
