@@ -309,10 +309,15 @@ def run_gpu(args):
     alg_bytes = BYTES_PER_CELL[args.storage] * cells
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     traffic = profiled_traffic() if args.storage == "f32" else None
+    ctype = {"f32": "float", "f64": "double", "f16": "half", "bf16": "bfloat16"}[args.storage]
+    shape = args.shape or (3 if args.storage in ("f16", "bf16") else 1)
+    kname = {1: f"k_beta/k_alpha<{ctype},LES> (one cell per thread)",
+             2: f"k_beta2/k_alpha2<{ctype},LES> (two cells per thread)",
+             3: f"k_step_staged<{ctype},LES> (TMA-staged tiles)"}[shape]
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": round(traffic * cells) if traffic else None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
-                "fallback 6.8 TB/s", "kernel": "k_beta/k_alpha<float,LES> (step kernel)",
+                "fallback 6.8 TB/s", "kernel": kname,
                 "kernel_ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": alg_bytes}
 
     prm = make_params(api, "f32")
