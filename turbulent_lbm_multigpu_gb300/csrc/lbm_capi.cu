@@ -266,9 +266,20 @@ __global__ void k_halo_one(HaloDesc h) {
     halo_elem<E>(h);
 }
 
-template <typename E>
-__global__ void k_halo_batch(const HaloDesc *__restrict__ hd) {
-    halo_elem<E>(hd[blockIdx.z]);
+// All copies of one exchange phase (up to N) in the kernel parameters:
+// their descriptor reads come from the constant bank (measured against a
+// descriptor array in global memory at 256^3 in 2x2x1 subdomains, float:
+// 16 instead of 30 registers, x faces 28.9 -> 27.2 us, y faces 10.8 ->
+// 8.1 us per phase).
+template <int N> struct HaloArgs {
+    HaloDesc h[N];
+};
+constexpr int kHaloParam = 64;
+static_assert(sizeof(HaloArgs<kHaloParam>) <= 32764, "halo descriptors exceed the kernel parameter space");
+
+template <typename E, int N>
+__global__ void k_halo_batch(const __grid_constant__ HaloArgs<N> a) {
+    halo_elem<E>(a.h[blockIdx.z]);
 }
 
 // Neumaier-compensated FP64 accumulation.
@@ -585,17 +596,36 @@ int launch_halo_one(const HaloDesc &h, cudaStream_t st) {
     return 0;
 }
 
-// All copies of one exchange phase in one launch.
-int launch_halo_batch(int storage, const HaloDesc *d_hd, int nd, int64_t max_cells, int max_planes, cudaStream_t st) {
-    if (nd <= 0 || max_cells <= 0) return 0;
-    const dim3 g = halo_grid(max_cells, max_planes, nd);
-    switch (storage_bytes(storage)) {
-        case 2: k_halo_batch<uint16_t><<<g, kBlock, 0, st>>>(d_hd); break;
-        case 4: k_halo_batch<uint32_t><<<g, kBlock, 0, st>>>(d_hd); break;
-        default: k_halo_batch<uint64_t><<<g, kBlock, 0, st>>>(d_hd); break;
-    }
+template <typename E, int N>
+static int launch_halo_param(const HaloDesc *hd, int n, int64_t max_cells, int max_planes, cudaStream_t st) {
+    HaloArgs<N> a;
+    memset(&a, 0, sizeof(a));
+    memcpy(a.h, hd, (size_t)n * sizeof(HaloDesc));
+    k_halo_batch<E, N><<<halo_grid(max_cells, max_planes, n), kBlock, 0, st>>>(a);
     CU(cudaGetLastError());
     return 0;
+}
+
+template <typename E>
+static int launch_halo_chunks(const HaloDesc *hd, int nd, int64_t max_cells, int max_planes, cudaStream_t st) {
+    for (int c0 = 0; c0 < nd; c0 += kHaloParam) {
+        const int n = std::min(kHaloParam, nd - c0);
+        const int rc = n <= 8 ? launch_halo_param<E, 8>(hd + c0, n, max_cells, max_planes, st)
+                              : launch_halo_param<E, kHaloParam>(hd + c0, n, max_cells, max_planes, st);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+// All copies of one exchange phase (independent of one another): one launch
+// per kHaloParam copies, descriptors from host memory.
+int launch_halo_batch(int storage, const HaloDesc *hd, int nd, int64_t max_cells, int max_planes, cudaStream_t st) {
+    if (nd <= 0 || max_cells <= 0) return 0;
+    switch (storage_bytes(storage)) {
+        case 2: return launch_halo_chunks<uint16_t>(hd, nd, max_cells, max_planes, st);
+        case 4: return launch_halo_chunks<uint32_t>(hd, nd, max_cells, max_planes, st);
+        default: return launch_halo_chunks<uint64_t>(hd, nd, max_cells, max_planes, st);
+    }
 }
 }  // namespace lbm_rt
 
@@ -972,7 +1002,6 @@ struct lbm_domain {
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
     std::vector<HaloDesc> plan[2][3];
-    HaloDesc *d_plan[2][3] = {};
     int64_t plan_cells[2][3] = {};
     int plan_planes[2][3] = {};
     int halo_mode = 0;  // 0: all 19 populations after alpha (reference), 1: the 5 read inward
@@ -1028,14 +1057,6 @@ int domain_build_plans(lbm_domain *D) {
             }
             D->plan_cells[ph][a] = cells;
             D->plan_planes[ph][a] = planes;
-            if (D->d_plan[ph][a]) {
-                cudaFree(D->d_plan[ph][a]);
-                D->d_plan[ph][a] = nullptr;
-            }
-            if (!v.empty()) {
-                CU(cudaMalloc((void **)&D->d_plan[ph][a], v.size() * sizeof(HaloDesc)));
-                CU(cudaMemcpy(D->d_plan[ph][a], v.data(), v.size() * sizeof(HaloDesc), cudaMemcpyHostToDevice));
-            }
         }
     return 0;
 }
@@ -1071,7 +1092,7 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
         if (!D->plan[parity][a].empty() &&
-            launch_halo_batch(D->storage, D->d_plan[parity][a], (int)D->plan[parity][a].size(), D->plan_cells[parity][a],
+            launch_halo_batch(D->storage, D->plan[parity][a].data(), (int)D->plan[parity][a].size(), D->plan_cells[parity][a],
                               D->plan_planes[parity][a], st))
             return -1;
     return 0;
@@ -1154,9 +1175,6 @@ int lbm_cu_domain_destroy(lbm_domain *D) {
     if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
     for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
     for (auto *l : D->subs) lbm_cu_destroy(l);
-    for (int p = 0; p < 2; p++)
-        for (int a = 0; a < 3; a++)
-            if (D->d_plan[p][a]) cudaFree(D->d_plan[p][a]);
     delete D;
     return 0;
 }
