@@ -1,6 +1,6 @@
 """Parity of the CUDA path (through the C ABI) with the oracle and the reference.
 
-Bar: bit-identical results.  The benchmark spec's tolerances (per-step population
+Bar: bit-identical results.  The project's parity tolerances (per-step population
 max-relative error 1e-6 in f32 and 1e-12 in f64) are asserted as well where a
 test compares floating-point fields, but the kernels are built to reproduce
 the reference arithmetic exactly and the tests demand equality of bits.
