@@ -73,6 +73,14 @@ const char *lbm_cu_version(void);
  * CLbmSolver::wait / clFinish (src/CLbmSolver.hpp:681-683). */
 int lbm_cu_synchronize(void *stream);
 
+/* Check of the staged kernels' failure path (no reference counterpart):
+ * launches one block whose bounded barrier wait (`polls` polls, at most the
+ * staged kernels' 2^22) runs out because nothing completes the barrier; the
+ * block records the timeout like a staged kernel that gave up waiting for
+ * its bulk copies and returns, so the next lbm_cu_synchronize fails with
+ * that message, clears it, and the device stays usable.  No fault, no trap. */
+int lbm_cu_check_wait_timeout(unsigned int polls, void *stream);
+
 /* ---------------------------------------------------------------- lattice */
 
 /* Allocate the fields of one nx*ny*nz lattice on the current device.

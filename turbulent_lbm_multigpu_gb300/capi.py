@@ -77,6 +77,7 @@ def lib() -> C.CDLL:
         "lbm_cu_last_error": ([], C.c_char_p),
         "lbm_cu_version": ([], C.c_char_p),
         "lbm_cu_synchronize": ([vp], ci),
+        "lbm_cu_check_wait_timeout": ([C.c_uint, vp], ci),
         "lbm_cu_create": ([ci, ci, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_destroy": ([vp], ci),
         "lbm_cu_dims": ([vp, ip], ci),
@@ -260,6 +261,18 @@ def compare_velocity(a: Lattice, layout_a: int, b: Lattice, layout_b: int, strea
 
 def halo(src: Lattice, src_origin, dst: Lattice, dst_origin, size, norm=None, stream=None):
     check(lib().lbm_cu_halo(src.h, ivec(src_origin), dst.h, ivec(dst_origin), ivec(size), ivec(norm), stream))
+
+
+def synchronize(stream=None):
+    """Wait for the stream (None: the device); raises LbmError if a staged
+    kernel gave up waiting for its bulk copies since the last call."""
+    check(lib().lbm_cu_synchronize(stream))
+
+
+def check_wait_timeout(polls=1 << 12, stream=None):
+    """Launch the bounded-wait check: its wait runs out by design and the
+    next synchronize() reports it."""
+    check(lib().lbm_cu_check_wait_timeout(polls, stream))
 
 
 class Domain:

@@ -629,6 +629,20 @@ int launch_halo_batch(int storage, const HaloDesc *hd, int nd, int64_t max_cells
 }
 }  // namespace lbm_rt
 
+// Check of the bounded waits: one block waits, `polls` polls at most, on a
+// barrier phase that nothing completes (no copy is issued), records
+// kStageTimeout in g_stage_error as the staged kernels do, and returns.
+static __global__ void k_wait_probe(uint32_t polls) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait(&bar, 0, polls);
+    if (!__any_sync(0xffffffffu, ok) && threadIdx.x == 0) atomicOr(&g_stage_error, kStageTimeout);
+}
+
 // =================================================================== C ABI
 extern "C" {
 
@@ -648,6 +662,13 @@ int lbm_cu_synchronize(void *stream) {
         CU(cudaMemcpyToSymbol(g_stage_error, &zero, sizeof(zero)));
         return fail("a staged step kernel gave up waiting for its bulk copies");
     }
+    return 0;
+}
+
+int lbm_cu_check_wait_timeout(unsigned int polls, void *stream) {
+    if (polls == 0 || polls > kStageWaitLimit) return fail("polls must be in 1..2^22");
+    k_wait_probe<<<1, 32, 0, S(stream)>>>(polls);
+    CU(cudaGetLastError());
     return 0;
 }
 
