@@ -201,6 +201,15 @@ int lbm_cu_checkpoint_load(lbm_lattice *lat, const char *path, int64_t *counter,
  * i / (nx*ny)) like the reference's rank mapping. */
 int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int store_velocity,
                          int store_density, int lid_geometry, lbm_domain **out);
+/* The same domain over lattices the caller already owns and initialised
+ * (one per subdomain, in subdomain order, each of the subdomain size, one
+ * storage type and the same stored fields): CManager's controllers run their
+ * lock-step time loop through it (one step launch over all subdomains and
+ * one halo launch per axis instead of one launch per subdomain and per
+ * CComm).  Destroying the view leaves the lattices alone; parameters set on
+ * a lattice directly take effect at the next lbm_cu_domain_run. */
+int lbm_cu_domain_wrap(lbm_lattice *const *subdomains, const int size[3], const int nums[3], int lid_geometry,
+                       lbm_domain **out);
 int lbm_cu_domain_destroy(lbm_domain *dom);
 int lbm_cu_domain_set_params(lbm_domain *dom, const lbm_params *p);
 /* init + geometry for all subdomains, step counter 0 (CLbmSolver::reset). */
@@ -233,6 +242,9 @@ int lbm_cu_domain_set_kernel_shape(lbm_domain *dom, int cells_per_thread);
 int lbm_cu_domain_profile(lbm_domain *dom, int enable);
 int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launches, int reset);
 int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
+/* Step counter of the next lbm_cu_domain_run (its parity picks beta or alpha;
+ * CLbmSolver::simulation_step_counter). */
+int lbm_cu_domain_set_counter(lbm_domain *dom, int64_t counter);
 int lbm_cu_domain_subdomains(const lbm_domain *dom, int *count, int sub_size[3]);
 lbm_lattice *lbm_cu_domain_lattice(lbm_domain *dom, int index);
 

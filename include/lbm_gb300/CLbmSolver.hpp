@@ -129,6 +129,8 @@ public:
 
     /** the device lattice (for halo exchanges) */
     lbm_lattice *lattice() { return lat; }
+    /** the stream every operation of this solver is issued on */
+    void *stream() const { return ctx.stream; }
     int getUid() const { return _UID; }
 
     void addDrivenCavityValue(T value) {

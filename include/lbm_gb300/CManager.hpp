@@ -6,12 +6,18 @@
 // The reference runs one subdomain per MPI rank; here initSimulation builds
 // every subdomain's controller in this process (on one GPU) and
 // startSimulation steps them in lock-step: all subdomains take the step,
-// then the halo exchange runs axis by axis.  `my_rank` selects the
-// controller getController() returns, so the reference's validate-mode flow
-// (src/main.cpp:309-408) keeps working.
+// then the halo exchange runs axis by axis.  The lock-step loop runs through
+// a domain view over the controllers' lattices (lbm_cu_domain_wrap: one step
+// launch over all subdomains, one halo launch per axis, CUDA-graph replay of
+// whole runs without per-step output) -- the same steps and copies as the
+// controllers' simulationStep / syncAlpha / syncBeta, which the environment
+// variable LBM_GB300_CONTROLLER_LOOP=1 selects instead.  `my_rank` selects
+// the controller getController() returns, so the reference's validate-mode
+// flow (src/main.cpp:309-408) keeps working.
 #ifndef LBM_GB300_CMANAGER_HPP
 #define LBM_GB300_CMANAGER_HPP
 
+#include <cstdlib>
 #include <iostream>
 #include <vector>
 
@@ -25,10 +31,36 @@ class CManager {
     CVector<3, int> _subdomain_nums;
     std::vector<CController<T> *> _controllers;
     int _rank = 0;
+    lbm_domain *_view = nullptr;  // all subdomains as one domain (nullptr: controller loop)
+
+    // The view when every solver issues on the same stream (else nullptr).
+    void buildView() {
+        const char *e = std::getenv("LBM_GB300_CONTROLLER_LOOP");
+        if (e && e[0] == '1') return;
+        std::vector<lbm_lattice *> subs;
+        for (auto *c : _controllers) {
+            if (c->getSolver()->stream() != _controllers[0]->getSolver()->stream()) return;
+            subs.push_back(c->getSolver()->lattice());
+        }
+        const CVector<3, int> s = _domain.getSize();
+        const int size[3] = {s[0], s[1], s[2]};
+        const int nums[3] = {_subdomain_nums[0], _subdomain_nums[1], _subdomain_nums[2]};
+        if (lbm_cu_domain_wrap(subs.data(), size, nums, 1, &_view)) _view = nullptr;
+    }
+
+    // `n` lock-step steps of every subdomain through the view.
+    void runView(int n, bool graph) {
+        CLbmSolver<T> *s0 = _controllers[0]->getSolver();
+        if (lbm_cu_domain_set_counter(_view, (int64_t)s0->simulation_step_counter) ||
+            lbm_cu_domain_run(_view, n, graph ? 1 : 0, s0->stream()))
+            throw lbm_cu_last_error();
+        for (auto *c : _controllers) c->getSolver()->simulation_step_counter += n;
+    }
 
 public:
     CManager(CDomain<T> domain, CVector<3, int> subdomainNums) : _domain(domain) { setSubdomainNums(subdomainNums); }
     ~CManager() {
+        if (_view) lbm_cu_domain_destroy(_view);  // a view: the lattices stay with the solvers
         for (auto *c : _controllers) delete c;
     }
     CManager(const CManager &) = delete;
@@ -80,10 +112,15 @@ public:
             _controllers.push_back(ctl);
         }
         for (auto *c : _controllers) c->setPeers(&_controllers);
+        buildView();
     }
 
     /** One time step of every subdomain followed by the halo exchange. */
     void step() {
+        if (_view) {
+            runView(1, false);
+            return;
+        }
         for (auto *c : _controllers) c->getSolver()->simulationStep();
         const bool beta = _controllers[0]->getSolver()->simulation_step_counter & 1;
         for (int axis = 0; axis < 3; axis++)
@@ -105,9 +142,17 @@ public:
             for (auto *c : _controllers) vis.push_back(c->newVisualization());
         CStopwatch sw;
         sw.start();
-        for (int i = 0; i < loops; i++) {
-            step();
-            for (auto *v : vis) v->render(i);
+        if (_view && vis.empty()) {
+            // nothing reads the fields between steps: velocity and density
+            // are written on the last step only, and pairs of steps replay
+            lbm_cu_domain_set_store_interval(_view, 0);
+            runView(loops, true);
+            lbm_cu_domain_set_store_interval(_view, 1);
+        } else {
+            for (int i = 0; i < loops; i++) {
+                step();
+                for (auto *v : vis) v->render(i);
+            }
         }
         for (auto *c : _controllers) c->getSolver()->wait();
         sw.stop();

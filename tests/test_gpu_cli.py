@@ -58,3 +58,25 @@ def test_cli_writes_vtk_snapshots_and_benchmark_record(capi, tmp_path):
     e = ini["EXP1"]
     assert (int(e["CUBE_X"]), int(e["CUBE_Y"]), int(e["CUBE_Z"])) == (16, 16, 16)
     assert float(e["MLUPS"]) > 0 and float(e["SECONDS"]) > 0 and float(e["FPS"]) > 0
+
+
+def test_cli_domain_view_equals_controller_loop(capi, tmp_path):
+    """The lock-step loop through the domain view (one step launch, one halo
+    launch per axis) writes the same VTK snapshots, byte for byte, as the
+    controllers' own simulationStep / syncAlpha / syncBeta loop."""
+    import os
+
+    exe = ROOT / "turbulent_lbm_multigpu_gb300" / "lbm_gb300"
+    outs = []
+    for loop in ("0", "1"):
+        d = tmp_path / f"loop{loop}"
+        d.mkdir()
+        env = dict(os.environ, LBM_GB300_CONTROLLER_LOOP=loop)
+        out = subprocess.run([str(exe), "-x", "24", "-y", "16", "-z", "16", "-X", "2", "-Y", "2", "-l", "5", "-g"],
+                             cwd=d, capture_output=True, text=True, timeout=300, env=env)
+        assert out.returncode == 0, out.stdout + out.stderr
+        outs.append(d / "output" / "vtk")
+    files = sorted(p.name for p in outs[0].iterdir())
+    assert len(files) == 4 * 5 and files == sorted(p.name for p in outs[1].iterdir())
+    for name in files:
+        assert (outs[0] / name).read_bytes() == (outs[1] / name).read_bytes(), name

@@ -201,6 +201,41 @@ def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, siz
             compare(api, O, L, s, storage, f"after step {R.counter}")
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_domain_view_over_own_lattices(capi, storage):
+    """lbm_cu_domain_wrap over lattices initialised elsewhere steps them
+    exactly as the owning domain does (graph replay, odd start counters, and
+    parameters changed through the lattices' own handles)."""
+    api = capi
+    size, nums = (48, 32, 16), (2, 2, 1)
+    st = api.STORAGE_NAMES[storage]
+
+    def made():
+        D = api.Domain(size, nums, st, True, True)
+        D.set_params(api.Params.make(1.0 / 0.56, 0.56, api.les_coefficient(0.17), (0, 0, 0), 0.08))
+        D.reset()
+        D.perturb(SEED, 1e-2)
+        return D
+
+    A, B = made(), made()
+    V = api.Domain.wrap(B.subdomains, size, nums)
+    A.run(7, True)
+    V.counter = 0
+    V.run(7, True)
+    assert V.counter == 7
+    p2 = api.Params.make(1.0 / 0.61, 0.61, api.les_coefficient(0.1), (0, 0, 0), 0.05)
+    A.set_params(p2)
+    for L in B.subdomains:
+        L.set_params(p2)
+    A.run(6, True)
+    V.run(6, True)
+    for La, Lb in zip(A.subdomains, B.subdomains):
+        for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY):
+            assert n_diff(La.read(f), Lb.read(f)) == 0
+    V.close()
+    assert n_diff(B.subdomains[0].read(api.FIELD_DD), A.subdomains[0].read(api.FIELD_DD)) == 0  # lattices kept
+
+
 def test_domain_equals_single_domain(capi, oracle_mod):
     """Validate mode on the GPU: decomposed interior velocity equals the
     reduced single domain bit for bit (src/main.cpp:309-408)."""

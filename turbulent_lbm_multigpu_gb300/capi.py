@@ -94,6 +94,8 @@ def lib() -> C.CDLL:
         "lbm_cu_compare_velocity": ([vp, ci, vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_domain_create": ([ip, ip, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_domain_destroy": ([vp], ci),
+        "lbm_cu_domain_wrap": ([C.POINTER(vp), ip, ip, ci, C.POINTER(vp)], ci),
+        "lbm_cu_domain_set_counter": ([vp, i64], ci),
         "lbm_cu_domain_set_params": ([vp, C.POINTER(Params)], ci),
         "lbm_cu_domain_reset": ([vp, vp], ci),
         "lbm_cu_domain_perturb": ([vp, u64, cd, vp], ci),
@@ -319,11 +321,30 @@ class Domain:
     def run(self, steps, use_graph=True, stream=None):
         check(lib().lbm_cu_domain_run(self.h, steps, int(use_graph), stream))
 
+    @classmethod
+    def wrap(cls, lattices, size, nums, lid_geometry=True):
+        """A view over lattices the caller owns and initialised, one per
+        subdomain in subdomain order (lbm_cu_domain_wrap)."""
+        self = cls.__new__(cls)
+        self.size, self.nums = tuple(size), tuple(nums)
+        self.storage = lattices[0].storage
+        arr = (C.c_void_p * len(lattices))(*[L.h.value for L in lattices])
+        h = C.c_void_p()
+        check(lib().lbm_cu_domain_wrap(arr, ivec(size), ivec(nums), int(lid_geometry), C.byref(h)))
+        self.h = h
+        self.sub = lattices[0].dims
+        self.subdomains = list(lattices)
+        return self
+
     @property
     def counter(self):
         c = C.c_int64()
         check(lib().lbm_cu_domain_counter(self.h, C.byref(c)))
         return c.value
+
+    @counter.setter
+    def counter(self, value):
+        check(lib().lbm_cu_domain_set_counter(self.h, int(value)))
 
     def set_store_interval(self, interval: int):
         check(lib().lbm_cu_domain_set_store_interval(self.h, interval))

@@ -1013,6 +1013,7 @@ struct CommGeom {
 struct lbm_domain {
     int size[3], nums[3], sub[3];
     int storage, store_v, store_rho, lid_geometry;
+    bool owns = true;  // false: a view over lattices the caller owns (lbm_cu_domain_wrap)
     std::vector<lbm_lattice *> subs;
     std::vector<std::vector<CommGeom>> comms;
     std::vector<std::vector<int>> bc;
@@ -1082,11 +1083,22 @@ int domain_build_plans(lbm_domain *D) {
     return 0;
 }
 
+int domain_geometry(lbm_domain *D);
+
+void drop_graph(lbm_domain *D);
+
 int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
     (void)st;
-    if (!D->tab_dirty) return 0;
-    D->h_tab.clear();
-    for (auto *l : D->subs) D->h_tab.push_back(l->h);
+    if (!D->tab_dirty && D->owns) return 0;
+    // a view's lattices may have changed parameters through their own handles:
+    // compare, and drop a graph captured with the old descriptors
+    std::vector<LatDesc> t;
+    for (auto *l : D->subs) t.push_back(l->h);
+    if (!D->tab_dirty && t.size() == D->h_tab.size() &&
+        memcmp(t.data(), D->h_tab.data(), t.size() * sizeof(LatDesc)) == 0)
+        return 0;
+    drop_graph(D);
+    D->h_tab.swap(t);
     D->eff_shape = effective_shape(D->storage, D->shape, D->h_tab.data(), (int)D->h_tab.size());
     D->tab_dirty = false;
     return 0;
@@ -1146,7 +1158,6 @@ int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int 
     D->store_rho = store_density ? 1 : 0;
     D->lid_geometry = lid_geometry;
     const int nsub = nums[0] * nums[1] * nums[2];
-    const int stride[3] = {1, nums[0], nums[0] * nums[1]};
     for (int id = 0; id < nsub; id++) {
         lbm_lattice *l = nullptr;
         if (lbm_cu_create(D->sub[0], D->sub[1], D->sub[2], storage, store_velocity, store_density, &l)) {
@@ -1155,6 +1166,72 @@ int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int 
             return fail(m);
         }
         D->subs.push_back(l);
+    }
+    if (domain_geometry(D)) {
+        std::string m = g_err;
+        lbm_cu_domain_destroy(D);
+        return fail(m);
+    }
+    *out = D;
+    return 0;
+}
+
+int lbm_cu_domain_wrap(lbm_lattice *const *subdomains, const int size[3], const int nums[3], int lid_geometry,
+                       lbm_domain **out) {
+    if (!subdomains || !size || !nums || !out) return fail("NULL argument");
+    *out = nullptr;
+    for (int a = 0; a < 3; a++) {
+        if (nums[a] < 1 || size[a] < 1) return fail("sizes and subdomain counts must be positive");
+        if (size[a] % nums[a] != 0) return fail("Number of subdomains does not match with the grid size!");
+    }
+    const int nsub = nums[0] * nums[1] * nums[2];
+    const lbm_lattice *l0 = subdomains[0];
+    for (int id = 0; id < nsub; id++) {
+        const lbm_lattice *l = subdomains[id];
+        if (!l) return fail("NULL subdomain lattice");
+        if (l->nx != size[0] / nums[0] || l->ny != size[1] / nums[1] || l->nz != size[2] / nums[2])
+            return fail("a subdomain lattice does not have the subdomain size");
+        if (l->storage != l0->storage || l->store_v != l0->store_v || l->store_rho != l0->store_rho)
+            return fail("subdomain lattices differ in storage type or stored fields");
+    }
+    lbm_domain *D = new lbm_domain();
+    D->owns = false;
+    for (int a = 0; a < 3; a++) {
+        D->size[a] = size[a];
+        D->nums[a] = nums[a];
+        D->sub[a] = size[a] / nums[a];
+    }
+    D->storage = l0->storage;
+    D->store_v = l0->store_v;
+    D->store_rho = l0->store_rho;
+    D->lid_geometry = lid_geometry;
+    D->subs.assign(subdomains, subdomains + nsub);
+    if (domain_geometry(D)) {
+        std::string m = g_err;
+        lbm_cu_domain_destroy(D);
+        return fail(m);
+    }
+    *out = D;
+    return 0;
+}
+
+int lbm_cu_domain_set_counter(lbm_domain *D, int64_t counter) {
+    if (!D) return fail("NULL domain");
+    if (counter < 0) return fail("negative step counter");
+    D->counter = counter;
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+// Faces of every subdomain (walls outside, ghost layers inside), its CComm
+// list in the reference's order and the halo plans (src/CManager.hpp:78-204).
+int domain_geometry(lbm_domain *D) {
+    const int *nums = D->nums;
+    const int nsub = nums[0] * nums[1] * nums[2];
+    const int stride[3] = {1, nums[0], nums[0] * nums[1]};
+    for (int id = 0; id < nsub; id++) {
         const int c[3] = {id % nums[0], (id / nums[0]) % nums[1], id / (nums[0] * nums[1])};
         D->coords.insert(D->coords.end(), c, c + 3);
         std::vector<int> bc(6, LBM_FLAG_GHOST_LAYER);
@@ -1181,21 +1258,19 @@ int lbm_cu_domain_create(const int size[3], const int nums[3], int storage, int 
         D->bc.push_back(bc);
         D->comms.push_back(cms);
     }
-    if (domain_build_plans(D)) {
-        std::string m = g_err;
-        lbm_cu_domain_destroy(D);
-        return fail(m);
-    }
-    *out = D;
-    return 0;
+    return domain_build_plans(D);
 }
+}  // namespace
+
+extern "C" {
 
 int lbm_cu_domain_destroy(lbm_domain *D) {
     if (!D) return 0;
     drop_graph(D);
     if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
     for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
-    for (auto *l : D->subs) lbm_cu_destroy(l);
+    if (D->owns)
+        for (auto *l : D->subs) lbm_cu_destroy(l);
     delete D;
     return 0;
 }
