@@ -80,3 +80,27 @@ def test_cli_domain_view_equals_controller_loop(capi, tmp_path):
     assert len(files) == 4 * 5 and files == sorted(p.name for p in outs[1].iterdir())
     for name in files:
         assert (outs[0] / name).read_bytes() == (outs[1] / name).read_bytes(), name
+
+
+@pytest.mark.parametrize("loop", ["0", "1"])
+def test_cli_validate_mode_passes(capi, tmp_path, loop):
+    """The reference's validate mode (src/main.cpp:309-408) through conf.xml:
+    the decomposed run's interior velocity equals the single domain's, cell
+    for cell, through the domain view (graph replay) and the controller loop."""
+    import os
+    import re
+
+    conf = (ROOT / "conf.xml").read_text()
+    for tag, val in (("loops", "30"), ("validate", "1")):
+        conf = re.sub(rf"<{tag}>[^<]*</{tag}>", f"<{tag}>{val}</{tag}>", conf, count=1)
+    conf = re.sub(r"<domain-size>.*?</domain-size>",
+                  "<domain-size><x>40</x><y>32</y><z>16</z></domain-size>", conf, flags=re.S)
+    conf = re.sub(r"<perturbation>[^<]*</perturbation>", "<perturbation>0</perturbation>", conf)
+    (tmp_path / "conf.xml").write_text(conf)
+    exe = ROOT / "turbulent_lbm_multigpu_gb300" / "lbm_gb300"
+    env = dict(os.environ, LBM_GB300_CONTROLLER_LOOP=loop)
+    out = subprocess.run([str(exe), "-c", "conf.xml"], cwd=tmp_path, capture_output=True, text=True,
+                         timeout=300, env=env)
+    assert out.returncode == 0, out.stdout + out.stderr
+    m = re.search(r"NUMBER OF FAILED CELLS/TOTAL NUMBER OF CELLS: (\d+)/(\d+)", out.stdout)
+    assert m and int(m.group(1)) == 0 and int(m.group(2)) == 18 * 14 * 14, out.stdout
