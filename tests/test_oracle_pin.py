@@ -57,6 +57,27 @@ def test_oracle_reproduces_reference_c1_hashes(oracle_mod, storage, wg):
         assert state_hash(s.lat.dd, s.lat.vel, s.lat.rho, s.lat.flags, m) == ref[k], f"step {k}"
 
 
+@pytest.mark.parametrize("plant", ["inv_tau", "lid"])
+def test_pin_detects_a_one_ulp_mistake(oracle_mod, plant):
+    """Negative control of the pin above: the oracle with one parameter moved
+    by one unit in the last place (a mistake planted on the CPU) leaves the
+    reference's hashes within a few steps."""
+    O = oracle_mod
+    ref = golden_hashes()["c1_f32"]
+    p = O.Params.lattice(O.cavity_tau(0.05, 64, 1000.0), 0.05, dtype=np.float32, wg=0)
+    if plant == "inv_tau":
+        p.inv_tau = float(np.nextafter(np.float32(p.inv_tau), np.float32(2)))
+    else:
+        p.lid = float(np.nextafter(np.float32(p.lid), np.float32(1)))
+    s = O.single(O.OracleKernels("f32"), (64, 64, 64), p, "f32")
+    m = O.fluid_mask(s.lat.flags)
+    differs = False
+    for k in range(1, min(len(ref), 6)):
+        s.step()
+        differs = differs or state_hash(s.lat.dd, s.lat.vel, s.lat.rho, s.lat.flags, m) != ref[k]
+    assert differs
+
+
 def test_oracle_reproduces_reference_decomposed_hashes(oracle_mod):
     O = oracle_mod
     ref = golden_hashes()["decomposed_f32"]
