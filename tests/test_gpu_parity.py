@@ -92,6 +92,31 @@ def test_steps_match_oracle(capi, oracle_mod, storage, cs, gravity, gmode, dims,
         compare(api, O, L, s, storage, f"after step {k + 1}")
 
 
+@pytest.mark.parametrize("storage,shape", [("f32", 1), ("f16", 3)])
+def test_parity_detects_a_planted_mistake(capi, oracle_mod, storage, shape):
+    """Negative control: with the oracle's BGK relaxation rate moved (the
+    mistake planted on the CPU side) -- by one unit in the last place for
+    float, by 2^-7 relative for half storage, whose 11-bit populations absorb
+    smaller changes -- the CUDA populations no longer match it."""
+    import dataclasses
+
+    api, O = capi, oracle_mod
+    dims = (64, 12, 18)
+    p = oracle_params(O, storage, dims)
+    L = gpu_single(api, O, dims, storage, p, perturb=(SEED, 2e-2))
+    L.set_kernel_shape(shape)
+    inv = np.float32(p.inv_tau)
+    inv = np.nextafter(inv, np.float32(2)) if storage == "f32" else np.float32(inv * (1 + 2.0 ** -7))
+    s = O.single(O.OracleKernels(storage), dims, dataclasses.replace(p, inv_tau=float(inv)), storage)
+    s.k.perturb(s.lat, (0, 0, 0), dims, SEED, 2e-2)
+    differs = 0
+    for _ in range(4):
+        L.step(s.lat.counter & 1)
+        s.step()
+        differs += n_diff(L.read(api.FIELD_DD), s.k.decode(s.lat.dd))
+    assert differs > 0
+
+
 @pytest.mark.parametrize("storage", ["f32", "f64"])
 def test_matches_reference_arrays(capi, oracle_mod, storage):
     """Full arrays written by the reference kernels (tests/golden)."""
