@@ -473,11 +473,16 @@ static int sm_count() {
 
 template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
 static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
-    static bool attr = false;  // the ring exceeds the default 48 KB of dynamic shared memory
-    if (!attr) {
+    // the ring exceeds the default 48 KB of dynamic shared memory; the limit
+    // is raised once per device
+    static bool attr[64] = {};
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail("device index out of range");
+    if (!attr[dev]) {
         CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 Tile<S>::SMEM));
-        attr = true;
+        attr[dev] = true;
     }
     const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
     k_step_staged<S, LES, BETA, ONE, N><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
