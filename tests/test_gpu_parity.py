@@ -207,7 +207,10 @@ def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph, sha
     ("bf16", (36, 24, 24), (2, 1, 3), 1),
     # subdomains 32 and 16 cells wide: the staged beta tiles (two cells per
     # thread with the subgrid model) run over ghost layers
-    ("f16", (64, 24, 20), (2, 2, 1), 1), ("bf16", (48, 16, 24), (3, 1, 2), 0)])
+    ("f16", (64, 24, 20), (2, 2, 1), 1), ("bf16", (48, 16, 24), (3, 1, 2), 0),
+    # 64 subdomains: 96 copies per exchange phase, more than one launch's
+    # parameter space holds
+    ("f32", (24, 24, 24), (4, 4, 4), 0), ("f16", (24, 24, 24), (4, 4, 4), 1)])
 def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, size, nums, halo_mode):
     api, O = capi, oracle_mod
     p = oracle_params(O, storage, (28, 0, 0), cs=0.17, re=5000.0, u=0.1)
