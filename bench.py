@@ -235,7 +235,7 @@ def make_params(api, storage):
     return api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
 
 
-def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None):
+def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None, halo_mode=HALO_MODE):
     """K timed steps of one domain with a CUDA-event pair around every step
     kernel; returns (wall ms of the K steps, step-kernel ms per launch,
     graph-replay MLUPS, cells)."""
@@ -243,7 +243,7 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, sha
 
     D = api.Domain(size, nums, api.STORAGE_NAMES[storage], store_velocity=False, store_density=False)
     D.set_params(make_params(api, storage))
-    D.set_halo_mode(HALO_MODE)
+    D.set_halo_mode(halo_mode)
     if shape:
         D.set_kernel_shape(shape)
     D.reset()
@@ -326,12 +326,14 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra and tuple(args.size) == SIZE:
         n = max(50, min(args.steps, 400))
-        for label, size, nums, st in (("f64 256^3 2x2x1", SIZE, NUMS, "f64"),
-                                      ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16"),
-                                      ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16"),
-                                      ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32"),
-                                      ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16")):
-            xms, xk, xg, xc = measure(api, size, nums, st, n, 4)
+        for label, size, nums, st, hm in (
+                ("f32 256^3 2x2x1, reference exchange (19 populations after alpha)", SIZE, NUMS, "f32", 0),
+                ("f64 256^3 2x2x1", SIZE, NUMS, "f64", HALO_MODE),
+                ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16", HALO_MODE),
+                ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16", HALO_MODE),
+                ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32", HALO_MODE),
+                ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16", HALO_MODE)):
+            xms, xk, xg, xc = measure(api, size, nums, st, n, 4, halo_mode=hm)
             xa = BYTES_PER_CELL[st] * xc / (xk * 1e-3) / 1e9
             extra[label] = {"mlups": round(xc * n / (xms * 1e-3) / 1e6, 1), "graph_mlups": round(xg, 1),
                             "kernel_ms": round(xk, 4), "achieved_gbs": round(xa, 1),

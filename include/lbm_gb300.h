@@ -176,8 +176,12 @@ int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int la
  * exits) and calls no allocator.  Limit: lattices of at most 134,217,728
  * cells (512^3); larger ones are rejected with an error.  The first call on
  * a device looks up the array's device address, so make that first call
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race and must be ordered by the caller. */
+ * before any stream capture.  With CUDA's lazy module loading that first
+ * call may also be what loads this part of the library onto the device (an
+ * implicit allocation of the array itself), so make one warm-up call on each
+ * device before handing out the rest of its memory.  All calls share the
+ * array: calls whose work overlaps on the GPU race and must be ordered by
+ * the caller. */
 int lbm_cu_reduce_conserved_noalloc(lbm_lattice *lat, int layout, double out[5], void *stream);
 
 /* Checkpoint / restart (no reference counterpart: the reference writes VTK

@@ -59,8 +59,8 @@ public:
                   (T)0.5;
         }
         if (tau < 0.51 || tau > 2.5) {
-            error << "tau has to be within the boundary [0.51; 2.5]" << std::endl;
-            error << "otherwise the simulation becomes unstable! current value: " << tau << std::endl;
+            error << "relaxation time " << tau << " outside the accepted window [0.51, 2.5]" << std::endl;
+            error << "(runs outside it are unstable; lattice units in conf.xml bypass this check)" << std::endl;
         }
         inv_tau = (T)1.0 / tau;
         inv_trt_tau = (T)1.0 / ((T)0.5 + (T)3.0 / ((T)16.0 * tau - (T)8.0));

@@ -22,7 +22,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 SHIM = HERE / "ref_shim"
-REF_DIR = Path(os.environ.get("LBM_REF_DIR", "/root/reference"))
+# the reference tree: LBM_REF_DIR, else a directory named "reference" beside
+# this repository's root
+REF_DIR = Path(os.environ.get("LBM_REF_DIR") or (HERE.parent.parent / "reference"))
 
 KINDS = {"lbm_init": 1, "lbm_alpha": 2, "lbm_beta": 3, "copy_buffer_rect": 4}
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference's own kernels.
 
-Run on a machine that has the reference tree (LBM_REF_DIR, default
-/root/reference):  python tests/golden/make_golden.py
+Run on a machine that has the reference tree (LBM_REF_DIR, default: the
+directory `reference` beside this repository):  python tests/golden/make_golden.py
 
 The reference kernels (src/cl_programs/*.cl) are compiled as C++ by
 oracle/build_ref.py and driven by the host logic of oracle/oracle.py.  The

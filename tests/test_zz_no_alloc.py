@@ -31,7 +31,7 @@ def _lattice(api, O, dims, storage, steps):
 
 
 @pytest.mark.parametrize("storage,dims,steps", [("f32", (48, 40, 36), 5), ("f64", (30, 26, 22), 4),
-                                                ("f16", (64, 64, 40), 3)])
+                                                ("f16", (64, 64, 40), 3), ("bf16", (64, 48, 40), 3)])
 def test_noalloc_sums_equal_allocating_sums(capi, oracle_mod, storage, dims, steps):
     api, O = capi, oracle_mod
     L = _lattice(api, O, dims, storage, steps)
@@ -56,3 +56,13 @@ def test_noalloc_rejects_lattices_beyond_its_limit(capi):
     L = api.Lattice(514, 512, 512, api.F16, False, False)  # 134,742,016 cells > 512^3
     with pytest.raises(api.LbmError, match="handles at most 134217728"):
         L.reduce_conserved_noalloc(0)
+
+
+def test_noalloc_at_its_limit(capi):
+    """A 512^3 lattice fills all 16384 partials of the array."""
+    api = capi
+    L = api.Lattice(512, 512, 512, api.F16, False, False)
+    L.init([api.FLAG_OBSTACLE] * 6)
+    L.perturb((0, 0, 0), (512, 512, 512), SEED, 3e-2)  # writes the opposite-slot layout
+    for _ in range(2):
+        np.testing.assert_allclose(L.reduce_conserved_noalloc(1), L.reduce_conserved(1), rtol=1e-12, atol=1e-13)

@@ -808,6 +808,31 @@ static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], voi
     }
     const size_t bytes = (size_t)cells * nplanes * ebytes;
     if (cells > INT32_MAX) return fail("rectangle has more than 2^31-1 cells");
+    // The whole lattice of a field whose host layout is its device layout
+    // (float / double populations: stored values are the populations; velocity
+    // and density planes of n cells): copy engine transfers straight between
+    // the host buffer and the planes, no staging buffer and no kernel.
+    const bool whole = o[0] == 0 && o[1] == 0 && o[2] == 0 && s[0] == l->nx && s[1] == l->ny && s[2] == l->nz;
+    if (whole && field != LBM_FIELD_FLAGS && (field != LBM_FIELD_DD || storage_bytes(l->storage) == rb)) {
+        const auto kind = read ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+        char *h = (char *)host;
+        if (field == LBM_FIELD_DD) {
+            const Planes pl = plane_list(read ? nullptr : norm);
+            const size_t pb = (size_t)l->n * rb;
+            for (int k = 0; k < pl.n; k++) {
+                const int f = pl.f[k];
+                char *dev = (char *)l->dd + (size_t)f * l->pstride * rb;
+                CU(cudaMemcpyAsync(read ? (void *)(h + f * pb) : (void *)dev, read ? (const void *)dev : h + f * pb, pb,
+                                   kind, st));
+            }
+        } else {
+            char *dev = (char *)(field == LBM_FIELD_VELOCITY ? l->vel : l->rho);
+            CU(cudaMemcpyAsync(read ? (void *)h : (void *)dev, read ? (const void *)dev : (const void *)h, bytes, kind,
+                               st));
+        }
+        CU(cudaStreamSynchronize(st));
+        return 0;
+    }
     if (ensure_stage(l, bytes + 256)) return -1;
     Box b = make_box(l, o, s);
     if (!read) CU(cudaMemcpyAsync(l->stage, host, bytes, cudaMemcpyHostToDevice, st));
@@ -963,6 +988,24 @@ constexpr int kStaticPartials = 16384;
 constexpr int64_t kStaticCellsPerBlock = (int64_t)kBlock * 32;
 static __device__ __align__(256) double g_reduce_scratch[kStaticPartials * 10 + 8];
 
+// Final stage over up to kStaticPartials partials: warp q sums quantity q,
+// each lane a strided share with its own compensated sum, then the lanes'
+// sums are merged by shuffles (one block of 5 warps; a single thread per
+// quantity would walk all 16384 partials one after another).
+__global__ void __launch_bounds__(160) k_reduce_final_warps(const double *partial, int nblocks, double *out) {
+    const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Acc a{0.0, 0.0};
+    for (int b = lane; b < nblocks; b += 32) {
+        a.add(partial[(b * 5 + q) * 2]);
+        a.c += partial[(b * 5 + q) * 2 + 1];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const Acc other{__shfl_down_sync(0xffffffffu, a.s, o), __shfl_down_sync(0xffffffffu, a.c, o)};
+        if (lane + o < 32) a.merge(other);
+    }
+    if (lane == 0) out[q] = a.s + a.c;
+}
+
 namespace {
 // Device address of g_reduce_scratch, looked up once per device with that
 // device current (the host-side symbol is not a device address).
@@ -1001,7 +1044,7 @@ extern "C" int lbm_cu_reduce_conserved_noalloc(lbm_lattice *l, int layout, doubl
         case kBF16: k_reduce<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
     }
     CU(cudaGetLastError());
-    k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, res);
+    k_reduce_final_warps<<<1, 160, 0, st>>>(partial, blocks, res);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));

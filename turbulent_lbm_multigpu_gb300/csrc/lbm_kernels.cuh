@@ -949,7 +949,11 @@ __global__ void __launch_bounds__(256, 2) k_alpha2(const __grid_constant__ Domai
 //          sources wrap) and a partial last tile take the one-cell path
 //          with the wrap instead.
 // Every wait on a barrier is bounded; a wait that runs out records
-// kStageTimeout in g_stage_error and the warp stops.
+// kStageTimeout in g_stage_error and the warp stops: a compute warp leaves
+// its loop (it issues no asynchronous copies of its own), the producer stops
+// issuing tiles, then waits -- bounded again -- until the loads it issued
+// have landed and its bulk stores are done, and only then returns, so no
+// copy into the block's shared memory outlives the block.
 constexpr int kStages = 3;
 constexpr int kStageBlocksPerSM = 3;
 constexpr int kConsumerWarps = 8;
@@ -1226,6 +1230,7 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
 
     if (warp == kConsumerWarps) {  // producer warp
         bool ok = true;
+        int staged = 0;  // tiles whose loads this warp has issued (ring slot k % kStages for tile k)
         const int rounds = mine + (BETA ? 0 : kStages);
         for (int k = 0; k < rounds; ++k) {
             const int s = k % kStages;
@@ -1236,9 +1241,23 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
                 if (!ok) break;
                 if (!BETA) unstage_tile<S, ONE, N>(a, blockIdx.x + (k - kStages) * stride, tile_lat[s], stage, lane);
             }
-            if (k < mine) stage_tile<S, BETA, ONE, N>(a, blockIdx.x + k * stride, stage, &full[s], &tile_lat[s], lane);
+            if (k < mine) {
+                stage_tile<S, BETA, ONE, N>(a, blockIdx.x + k * stride, stage, &full[s], &tile_lat[s], lane);
+                staged = k + 1;
+            }
         }
-        if (!ok && lane == 0) atomicOr(&g_stage_error, kStageTimeout);
+        // Leave only after every load this warp issued has landed: the block's
+        // shared memory must outlive the copies into it, and the compute warps
+        // may already have left (normally they consume the last tiles, but one
+        // that ran out of time on a "full" barrier does not).  Each buffer has at
+        // most one armed phase that nobody may have waited for: the one of the
+        // last tile staged into it.  These waits are bounded as well.
+        bool drained = true;
+        for (int s = 0; s < kStages && s < staged; s++) {
+            const int k_last = s + kStages * ((staged - 1 - s) / kStages);
+            drained &= mbar_wait(&full[s], (uint32_t)((k_last / kStages) & 1));
+        }
+        if ((!ok || !drained) && lane == 0) atomicOr(&g_stage_error, kStageTimeout);
         bulk_wait_all();
         return;
     }
