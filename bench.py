@@ -42,7 +42,7 @@ METRIC = "D3Q19 MLUPS & % HBM roofline; served solves/s, p50/p99 latency vs plai
 SIZE = (256, 256, 256)
 NUMS = (2, 2, 1)
 U_LID, RE, CS, SEED, AMP = 0.1, 10000.0, 0.17, 1234, 1e-3
-BYTES_PER_CELL = {"f32": 152, "f64": 304, "f16": 76, "bf16": 76}
+BYTES_PER_CELL = {"f32": 152, "f64": 304, "f16": 76, "bf16": 76, "c16": 76}
 HALO_MODE = 1  # after alpha, exchange the 5 populations the ghost layer's inner neighbours read
 
 
@@ -235,7 +235,8 @@ def make_params(api, storage):
     return api.Params.make(pp["inv_tau"], pp["tau0"], pp["les_c"], (0.0, 0.0, 0.0), pp["lid"])
 
 
-def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None, halo_mode=HALO_MODE):
+def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None, halo_mode=HALO_MODE,
+            fp64_fma=False):
     """K timed steps of one domain with a CUDA-event pair around every step
     kernel; returns (wall ms of the K steps, step-kernel ms per launch,
     graph-replay MLUPS, cells)."""
@@ -246,6 +247,8 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, sha
     D.set_halo_mode(halo_mode)
     if shape:
         D.set_kernel_shape(shape)
+    if fp64_fma:
+        D.set_fp64_contraction(True)
     D.reset()
     D.perturb(SEED, AMP)
     D.run(warmup, use_graph=False)
@@ -298,7 +301,7 @@ def run_gpu(args):
 
     with ClockSampler(local) as clk:
         ms, k_ms, graph_mlups, cells = measure(api, args.size, args.nums, args.storage, args.steps, args.warmup, dist,
-                                               shape=args.shape)
+                                               shape=args.shape, fp64_fma=args.fp64_fma)
     ms = max_over_ranks(ms, dist)
     mlups = whole_job_mlups(cells, args.steps, ms, ws)
     if args.steps < 2:
@@ -309,8 +312,8 @@ def run_gpu(args):
     alg_bytes = BYTES_PER_CELL[args.storage] * cells
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     traffic = profiled_traffic() if args.storage == "f32" else None
-    ctype = {"f32": "float", "f64": "double", "f16": "half", "bf16": "bfloat16"}[args.storage]
-    shape = args.shape or (3 if args.storage in ("f16", "bf16") else 1)
+    ctype = {"f32": "float", "f64": "double", "f16": "half", "bf16": "bfloat16", "c16": "c16_t"}[args.storage]
+    shape = args.shape or (3 if args.storage in ("f16", "bf16", "c16") else 1)
     kname = {1: f"k_beta/k_alpha<{ctype},LES> (one cell per thread)",
              2: f"k_beta2/k_alpha2<{ctype},LES> (two cells per thread)",
              3: f"k_step_staged<{ctype},LES> (TMA-staged tiles)"}[shape]
@@ -326,14 +329,17 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra and tuple(args.size) == SIZE:
         n = max(50, min(args.steps, 400))
-        for label, size, nums, st, hm in (
-                ("f32 256^3 2x2x1, reference exchange (19 populations after alpha)", SIZE, NUMS, "f32", 0),
-                ("f64 256^3 2x2x1", SIZE, NUMS, "f64", HALO_MODE),
-                ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16", HALO_MODE),
-                ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16", HALO_MODE),
-                ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32", HALO_MODE),
-                ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16", HALO_MODE)):
-            xms, xk, xg, xc = measure(api, size, nums, st, n, 4, halo_mode=hm)
+        for label, size, nums, st, hm, fma in (
+                ("f32 256^3 2x2x1, reference exchange (19 populations after alpha)", SIZE, NUMS, "f32", 0, False),
+                ("f64 256^3 2x2x1", SIZE, NUMS, "f64", HALO_MODE, False),
+                ("f64 256^3 2x2x1, contracted multiply-adds (<= 1e-12 per step)", SIZE, NUMS, "f64", HALO_MODE, True),
+                ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16", HALO_MODE, False),
+                ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16", HALO_MODE, False),
+                ("c16-shifted 256^3 2x2x1 (13-bit significand)", SIZE, NUMS, "c16", HALO_MODE, False),
+                ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32", HALO_MODE, False),
+                ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16", HALO_MODE, False),
+                ("c16-shifted 512^3", (512, 512, 512), (1, 1, 1), "c16", HALO_MODE, False)):
+            xms, xk, xg, xc = measure(api, size, nums, st, n, 4, halo_mode=hm, fp64_fma=fma)
             xa = BYTES_PER_CELL[st] * xc / (xk * 1e-3) / 1e9
             extra[label] = {"mlups": round(xc * n / (xms * 1e-3) / 1e6, 1), "graph_mlups": round(xg, 1),
                             "kernel_ms": round(xk, 4), "achieved_gbs": round(xa, 1),
@@ -347,7 +353,7 @@ def run_gpu(args):
         extra["batch 512 cavities (steps/10)"] = {k: (round(v, 3) if isinstance(v, float) else v)
                                                  for k, v in b.items() if k != "config"}
         extra["batch 512 cavities (steps/10)"]["cell_updates"] = b["config"]["cell_updates"]
-        sv = ex.serve(requests=24, scale=4.0, rates=(100, 400))
+        sv = ex.serve(requests=24, scale=4.0, rates=(100, 400), accuracy_samples=0, f32_rate=None)
         extra["serving 24 requests (steps/4)"] = {
             "sequential_plain_f32_solves_per_s": round(sv["sequential_plain_f32"]["solves_per_s"], 3),
             "served": [{k: round(v, 4) for k, v in r.items()} for r in sv["served"]],
@@ -431,10 +437,12 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the extra storage / size measurements")
     ap.add_argument("--size", type=int, nargs=3, default=list(SIZE), help="domain size (profiling only)")
     ap.add_argument("--nums", type=int, nargs=3, default=list(NUMS), help="subdomains (profiling only)")
-    ap.add_argument("--storage", default="f32", choices=["f32", "f64", "f16", "bf16"],
+    ap.add_argument("--storage", default="f32", choices=["f32", "f64", "f16", "bf16", "c16"],
                     help="population storage of the main measurement (profiling only)")
     ap.add_argument("--shape", type=int, default=None, choices=[1, 2, 3],
                     help="step kernel shape of the main measurement (profiling only)")
+    ap.add_argument("--fp64-fma", action="store_true",
+                    help="double storage: contracted multiply-add kernels in the main measurement (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -29,9 +29,12 @@ extern "C" {
 #define LBM_FLAG_GHOST_LAYER 8
 
 /* Population storage.  F32/F64 correspond to the reference's T = float /
- * double.  F16/BF16 store the shifted deviations f_i - w_i and compute in
- * float (no reference counterpart). */
-enum lbm_storage { LBM_F32 = 0, LBM_F64 = 1, LBM_F16 = 2, LBM_BF16 = 3 };
+ * double.  F16/BF16/C16 store the shifted deviations f_i - w_i in 16 bits and
+ * compute in float (no reference counterpart).  C16 is a 16-bit float of this
+ * project with a 13-bit significand (1 sign, 3 exponent, 12 fraction bits;
+ * |f_i - w_i| < 1/16, larger values saturate): finer than binary16 within
+ * the range the deviations of a flow with |u| < ~0.28 occupy. */
+enum lbm_storage { LBM_F32 = 0, LBM_F64 = 1, LBM_F16 = 2, LBM_BF16 = 3, LBM_C16 = 4 };
 
 /* Fields for rectangular reads and writes. */
 enum lbm_field {
@@ -129,9 +132,19 @@ int lbm_cu_step(lbm_lattice *lat, int parity, void *stream);
  * src/CLbmSolver.hpp:279-312, tunes its OpenCL launch instead). */
 int lbm_cu_set_kernel_shape(lbm_lattice *lat, int cells_per_thread);
 
+/* Double lattices only: enable != 0 runs the step with kernels whose FP64
+ * products may fuse into the following sum (one rounding instead of two);
+ * 0 (default) keeps the bit-exact reference arithmetic.  A contracted step
+ * differs from the reference's by a relative 1e-15 (bound: 1e-12 per step),
+ * and runs faster because the double kernels are bound by the FP64 pipe.
+ * One cell per thread; overrides the kernel shape.  No reference counterpart
+ * (the reference builds its double kernels with the OpenCL compiler's
+ * defaults, src/CLbmSolver.hpp:319-373). */
+int lbm_cu_set_fp64_contraction(lbm_lattice *lat, int enable);
+
 /* Rectangular copy of one field between the lattice and a HOST buffer laid
  * out [plane][z][y][x] of size[0]*size[1]*size[2] cells per plane, elements
- * of the arithmetic type (float for F32/F16/BF16, double for F64) or int32
+ * of the arithmetic type (float for F32/F16/BF16/C16, double for F64) or int32
  * for flags.  Blocking, like the reference's CL_TRUE reads.  Replaces
  * storeDensityDistribution / storeVelocity / storeDensity / storeFlags and
  * their set* counterparts, with or without a rectangle
@@ -165,6 +178,13 @@ int lbm_cu_reduce_conserved(lbm_lattice *lat, int layout, double out[5], void *s
  * run; no reference counterpart. */
 int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int layout_b, double out[5],
                             void *stream);
+
+/* How the stored deviations of a 16-bit lattice (F16, BF16, C16) use their
+ * format, over the 19 slots of the fluid cells: out = {values, zeros,
+ * subnormals (nonzero below the smallest normal magnitude), values at the
+ * largest finite magnitude or beyond, largest |f_i - w_i|}.  For precision
+ * studies; no reference counterpart. */
+int lbm_cu_deviation_stats(lbm_lattice *lat, double out[5], void *stream);
 
 /* The same sums, for callers that must not allocate device memory (no
  * counterpart in the reference).  lbm_cu_reduce_conserved may grow the
@@ -237,8 +257,20 @@ int lbm_cu_domain_set_store_interval(lbm_domain *dom, int interval);
  * Both give identical fluid, lid and wall cells; ghost-layer populations
  * differ in the 14 slots no other cell reads. */
 int lbm_cu_domain_set_halo_mode(lbm_domain *dom, int mode);
+/* enable != 0 (default): where the subdomains run the one-cell kernels
+ * (kernel shape 1, the default for float and double), each alpha step also
+ * does the x part of the exchange after it -- the thread of a cell at
+ * x = nx-2 (x = 1) copies that cell's exchanged planes straight into the
+ * ghost cell x = 0 (x = nx-1) of its x neighbour -- instead of a separate
+ * copy launch that reads the face back.  The results are identical; the y
+ * and z parts still follow in their own launches, so the corners travel in
+ * two hops as in CController::syncAlpha (src/CController.hpp:265-320).
+ * 0: the x part runs as its own launch. */
+int lbm_cu_domain_set_fused_exchange(lbm_domain *dom, int enable);
 /* Kernel shape of every subdomain's step (see lbm_cu_set_kernel_shape). */
 int lbm_cu_domain_set_kernel_shape(lbm_domain *dom, int cells_per_thread);
+/* Contracted FP64 kernels for every subdomain (see lbm_cu_set_fp64_contraction). */
+int lbm_cu_domain_set_fp64_contraction(lbm_domain *dom, int enable);
 /* Time every step-kernel launch with a pair of CUDA events on the launching
  * stream (steps then run without graph replay), and read the accumulated
  * milliseconds and launch count (reset != 0 clears them).  Stands in for the

@@ -72,6 +72,7 @@ class CController {
             opt.smagorinsky = cfg->smagorinsky;
             if (cfg->storage == "f16") opt.storage = LBM_F16;
             else if (cfg->storage == "bf16") opt.storage = LBM_BF16;
+            else if (cfg->storage == "c16") opt.storage = LBM_C16;
         }
         const bool store = cfg->do_visualization || cfg->debug_mode;
         cLbmPtr = new CLbmSolver<T>(_UID, _ctx, _BC, _domain, cfg->gravitation, cfg->viscosity,

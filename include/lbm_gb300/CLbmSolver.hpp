@@ -33,7 +33,7 @@ struct CDeviceContext {
 /** Options with no counterpart in the reference. */
 template <typename T>
 struct CLbmOptions {
-    int storage = -1;           // LBM_F32/F64 from T when -1; LBM_F16/BF16 need T = float
+    int storage = -1;           // LBM_F32/F64 from T when -1; LBM_F16/BF16/C16 need T = float
     T smagorinsky = T(0);       // Cs; 0 keeps the reference's plain BGK
     bool lattice_units = false; // take tau and the lid speed below as given
     T lattice_tau = T(0);

@@ -30,7 +30,7 @@
  * inserted into the reference BGK update in place of the constant inv_tau.
  *
  * The file is compiled once per storage variant (VARIANT = 0 f32, 1 f64,
- * 2 shifted f16, 3 shifted bf16).  Shifted variants store g_i = f_i - w_i
+ * 2 shifted f16, 3 shifted bf16, 4 shifted c16).  Shifted variants store g_i = f_i - w_i
  * and do all arithmetic in float, in deviation form: the same model with
  * the operations the GB300 kernels perform for these types (pair sums,
  * explicit fused multiply-adds via fmaf, see dev_* below).  The reference
@@ -65,10 +65,15 @@ typedef float REAL;
 typedef _Float16 STOR;
 #define SFX(n) n##_f16
 #define SHIFTED 1
-#else
+#elif VARIANT == 3
 typedef float REAL;
 typedef uint16_t STOR;
 #define SFX(n) n##_bf16
+#define SHIFTED 1
+#else
+typedef float REAL;
+typedef uint16_t STOR;
+#define SFX(n) n##_c16
 #define SHIFTED 1
 #endif
 
@@ -116,6 +121,35 @@ static inline uint16_t f_to_bf16(float f) {
 #define STV(v, i) (f_to_bf16((v) - weight(i)))
 #define LDD(p) (bf16_to_f(p))
 #define STD(v) (f_to_bf16(v))
+#elif VARIANT == 4
+/* c16, this project's 16-bit float for the deviations (no reference
+ * counterpart): sign, 3 exponent bits e, 12 fraction bits m; e = 1..7 gives
+ * (1 + m/2^12) 2^(e-12), e = 0 gives m 2^-23; |g| < 2^-4, larger magnitudes
+ * saturate.  It is float's bit layout with the exponents moved down by 115
+ * binades.  Encoding scales |g| by 2^-115 (one float rounding, which only
+ * values in the subnormal range undergo), then rounds the float's fraction
+ * to 12 bits, halves away from zero; decoding places the bits into a float
+ * and scales back by 2^115 (exact).  Needs subnormal floats (no flush to
+ * zero). */
+static inline REAL c16_dec(uint16_t c) {
+    int32_t w = (int32_t)((uint32_t)c << 16);
+    uint32_t u = (uint32_t)(w >> 5) & 0x83fff800u; /* arithmetic shift: the sign stays in bit 31 */
+    float x;
+    memcpy(&x, &u, 4);
+    return x * 0x1p115f;
+}
+static inline uint16_t c16_enc(REAL v) {
+    float x = fabsf(v) * 0x1p-115f;
+    uint32_t a, u;
+    memcpy(&a, &x, 4);
+    memcpy(&u, &v, 4);
+    uint32_t r = (a + 0x400u) >> 11;
+    return (uint16_t)(((u >> 16) & 0x8000u) | (r < 0x7fffu ? r : 0x7fffu));
+}
+#define LD(p, i) (c16_dec(p) + weight(i))
+#define STV(v, i) (c16_enc((v) - weight(i)))
+#define LDD(p) (c16_dec(p))
+#define STD(v) (c16_enc(v))
 #elif VARIANT == 2
 #define LD(p, i) ((REAL)(p) + weight(i))
 #define STV(v, i) ((STOR)((v) - weight(i)))
@@ -278,8 +312,9 @@ static REAL gravity_chain(REAL rho, REAL gx, REAL gy, REAL gz, REAL t[9], int gm
  *   A = dd_param - 1 = (rho - 1) - 3/2 |u|^2,
  *   f_i^eq - w_i = w_i (A + 3 e_i.u + 9/2 (e_i.u)^2),
  *   g_i' = (1 - omega) g_i + omega (f_i^eq - w_i),
- * per opposite pair (2k, 2k+1) as P +- Q, P = omega w (A + 9/2 s^2),
- * Q = 3 omega w s, s = e_2k.u.  CW = sum of the float weights - 1 = 2^-26 and
+ * per opposite pair (2k, 2k+1) as P +- Q, P = omega w A + (9/2 omega w s) s,
+ * Q = 3 omega w s, s = e_2k.u, Q folded into each population's last fused
+ * multiply-add.  CW = sum of the float weights - 1 = 2^-26 and
  * CP = 2 w18 + 8 w36 - (float)(1/3) = -2^-27 keep the float weights' exact
  * offsets, so the model is the reference's one.  Subgrid rate:
  *   Pi_ab = sum e_a e_b g + CP delta - (rho - 1)/3 delta - u_a u_b,
@@ -307,26 +342,27 @@ static void dev_moments(const REAL g[19], REAL *dl, REAL *jx, REAL *jy, REAL *jz
     m2[5] = s[6] - s[7];
 }
 
-static void dev_pair(REAL g[19], int k, REAL v, REAL a, REAL b, REAL A, REAL om1) {
-    REAL h = fmaf(K45 * v, v, A);
-    REAL P = a * h, Q = b * v;
-    g[2 * k] = fmaf(om1, g[2 * k], P + Q);
-    g[2 * k + 1] = fmaf(om1, g[2 * k + 1], P - Q);
+static void dev_pair(REAL g[19], int k, REAL v, REAL aA, REAL a45, REAL b, REAL om1) {
+    REAL P = fmaf(a45 * v, v, aA);
+    g[2 * k] = fmaf(b, v, fmaf(om1, g[2 * k], P));
+    g[2 * k + 1] = fmaf(-b, v, fmaf(om1, g[2 * k + 1], P));
 }
 
 static void dev_relax(REAL g[19], REAL om, REAL A, REAL vx, REAL vy, REAL vz) {
     REAL om1 = (REAL)1.0f - om;
     REAL a18 = om * C18, a36 = om * C36, a3 = om * C3;
     REAL b18 = K3 * a18, b36 = K3 * a36;
-    dev_pair(g, 0, vx, a18, b18, A, om1);
-    dev_pair(g, 1, vy, a18, b18, A, om1);
-    dev_pair(g, 2, vx + vy, a36, b36, A, om1);
-    dev_pair(g, 3, vx - vy, a36, b36, A, om1);
-    dev_pair(g, 4, vx + vz, a36, b36, A, om1);
-    dev_pair(g, 5, vx - vz, a36, b36, A, om1);
-    dev_pair(g, 6, vy + vz, a36, b36, A, om1);
-    dev_pair(g, 7, vy - vz, a36, b36, A, om1);
-    dev_pair(g, 8, vz, a18, b18, A, om1);
+    REAL aA18 = a18 * A, aA36 = a36 * A;
+    REAL h18 = K45 * a18, h36 = K45 * a36;
+    dev_pair(g, 0, vx, aA18, h18, b18, om1);
+    dev_pair(g, 1, vy, aA18, h18, b18, om1);
+    dev_pair(g, 2, vx + vy, aA36, h36, b36, om1);
+    dev_pair(g, 3, vx - vy, aA36, h36, b36, om1);
+    dev_pair(g, 4, vx + vz, aA36, h36, b36, om1);
+    dev_pair(g, 5, vx - vz, aA36, h36, b36, om1);
+    dev_pair(g, 6, vy + vz, aA36, h36, b36, om1);
+    dev_pair(g, 7, vy - vz, aA36, h36, b36, om1);
+    dev_pair(g, 8, vz, aA18, h18, b18, om1);
     g[18] = fmaf(om1, g[18], a3 * A);
 }
 
@@ -671,3 +707,15 @@ void SFX(orc_encode)(const REAL *in, STOR *dd, int64_t n) {
     for (int i = 0; i < 19; i++)
         for (int64_t c = 0; c < n; c++) dd[i * n + c] = STV(in[i * n + c], i);
 }
+
+#if VARIANT == 4
+/* The c16 format alone (no weight shift): for the format's own tests. */
+void orc_c16_encode_raw(const float *in, uint16_t *out, int64_t n);
+void orc_c16_decode_raw(const uint16_t *in, float *out, int64_t n);
+void orc_c16_encode_raw(const float *in, uint16_t *out, int64_t n) {
+    for (int64_t k = 0; k < n; k++) out[k] = c16_enc(in[k]);
+}
+void orc_c16_decode_raw(const uint16_t *in, float *out, int64_t n) {
+    for (int64_t k = 0; k < n; k++) out[k] = c16_dec(in[k]);
+}
+#endif

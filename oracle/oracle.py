@@ -50,9 +50,10 @@ STORAGE = {  # name -> (storage numpy dtype, arithmetic numpy dtype)
     "f64": (np.float64, np.float64),
     "f16": (np.float16, np.float32),
     "bf16": (np.uint16, np.float32),
+    "c16": (np.uint16, np.float32),
 }
 
-_VARIANTS = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3}
+_VARIANTS = {"f32": 0, "f64": 1, "f16": 2, "bf16": 3, "c16": 4}
 
 
 def build(force: bool = False) -> Path:

@@ -38,7 +38,9 @@ def mix(api):
             C((10, 30, 12), api.F32, 0.58, 0.17, 0.05, 11, 19, 1e-2),
             # rows of whole 16-byte units: with shape 3 their beta steps are staged too
             C((32, 12, 14), api.F16, 0.54, 0.17, 0.06, 19, 20, 1e-2),
-            C((16, 20, 18), api.F16, 0.57, 0.17, 0.04, 15, 21, 1e-2)]
+            C((16, 20, 18), api.F16, 0.57, 0.17, 0.04, 15, 21, 1e-2),
+            C((32, 14, 12), api.C16, 0.55, 0.17, 0.07, 16, 22, 1e-2),
+            C((21, 16, 13), api.C16, 0.6, 0.17, 0.05, 12, 23, 1e-2)]
 
 
 @pytest.mark.parametrize("shape,use_graph", [(1, True), (2, True), (1, False), (3, True), (3, False)])

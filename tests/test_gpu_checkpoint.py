@@ -29,7 +29,7 @@ def cavity(api, dims, storage):
     return L
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16", "c16"])
 @pytest.mark.parametrize("first", [6, 7])
 def test_lattice_restart_is_bit_exact(capi, tmp_path, storage, first):
     api = capi

@@ -19,7 +19,7 @@ def params(api, storage, cs=0.17, tau=0.53):
     return api.Params.make(inv, float(t), api.les_coefficient(cs), (0.0, 0.0, 0.0), 0.07)
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16", "c16"])
 @pytest.mark.parametrize("dims", [(3, 3, 3), (4, 3, 5), (3, 7, 3), (9, 3, 4)])
 @pytest.mark.parametrize("shape", [1, 2, 3])
 def test_smallest_lattices_match_oracle(capi, oracle_mod, storage, dims, shape):

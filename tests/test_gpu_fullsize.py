@@ -26,7 +26,7 @@ pytestmark = pytest.mark.gpu
 
 SEED, AMP = 1234, 1e-3
 U_LID, RE, CS = 0.1, 1e4, 0.17
-TOL = {"f32": 1e-6, "f64": 1e-12, "f16": 1e-6, "bf16": 1e-6}
+TOL = {"f32": 1e-6, "f64": 1e-12, "f16": 1e-6, "bf16": 1e-6, "c16": 1e-6}
 
 
 def same(a, b) -> bool:
@@ -61,7 +61,7 @@ def check_lattice(api, L, sol, storage, where, fields=True, slab=64):
 
 
 @pytest.mark.parametrize("storage,halo_mode", [("f32", 0), ("f32", 1), ("f64", 1), ("f64", 0), ("f16", 1),
-                                               ("bf16", 0)])
+                                               ("bf16", 0), ("c16", 1)])
 def test_cavity_256cube_2x2x1_matches_oracle(capi, oracle_mod, storage, halo_mode):
     api, O = capi, oracle_mod
     size, nums = (256, 256, 256), (2, 2, 1)
@@ -91,7 +91,7 @@ def test_cavity_256cube_2x2x1_matches_oracle(capi, oracle_mod, storage, halo_mod
             check_lattice(api, L, s, storage, f"after step {R.counter} (graph replay)")
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("storage", ["f32", "f16", "c16"])
 def test_lattice_512cube_matches_oracle(capi, oracle_mod, storage):
     """One 512^3 lattice (19 x 134M population elements: 64-bit plane
     offsets), the benchmark's default kernel shape, four steps."""

@@ -15,7 +15,7 @@ from helpers import golden_hashes, golden_small, max_rel, n_diff, state_hash
 pytestmark = pytest.mark.gpu
 
 SEED = 1234
-TOL = {"f32": 1e-6, "f64": 1e-12, "f16": 1e-6, "bf16": 1e-6}
+TOL = {"f32": 1e-6, "f64": 1e-12, "f16": 1e-6, "bf16": 1e-6, "c16": 1e-6}
 
 
 def gpu_params(api, p):
@@ -56,7 +56,7 @@ def oracle_params(O, storage, dims, cs=0.0, gravity=(0.0, 0.0, 0.0), re=300.0, u
                             gravity=tuple(float(rdt(g)) for g in gravity), gravity_mode=gravity_mode)
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16", "c16"])
 def test_init_matches_oracle(capi, oracle_mod, storage):
     api, O = capi, oracle_mod
     dims = (13, 11, 9)
@@ -67,7 +67,7 @@ def test_init_matches_oracle(capi, oracle_mod, storage):
     compare(api, O, L, s, storage, "after init")
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "bf16", "c16"])
 @pytest.mark.parametrize("cs", [0.0, 0.17])
 @pytest.mark.parametrize("gravity,gmode", [((0.0, 0.0, 0.0), 0), ((1e-5, -2e-5, 3e-6), 0),
                                            ((1e-5, -2e-5, 3e-6), 1)])
@@ -210,7 +210,9 @@ def test_domain_matches_reference_decomposition(capi, oracle_mod, use_graph, sha
     ("f16", (64, 24, 20), (2, 2, 1), 1), ("bf16", (48, 16, 24), (3, 1, 2), 0),
     # 64 subdomains: 96 copies per exchange phase, more than one launch's
     # parameter space holds
-    ("f32", (24, 24, 24), (4, 4, 4), 0), ("f16", (24, 24, 24), (4, 4, 4), 1)])
+    ("f32", (24, 24, 24), (4, 4, 4), 0), ("f16", (24, 24, 24), (4, 4, 4), 1),
+    # the 16-bit float of this project, staged beta tiles over ghost layers
+    ("c16", (64, 24, 20), (2, 2, 1), 1), ("c16", (30, 20, 12), (2, 2, 1), 0)])
 def test_domain_matches_oracle_with_subgrid_model(capi, oracle_mod, storage, size, nums, halo_mode):
     api, O = capi, oracle_mod
     p = oracle_params(O, storage, (28, 0, 0), cs=0.17, re=5000.0, u=0.1)
@@ -341,7 +343,7 @@ def test_halo_copies_selected_planes(capi):
         assert n_diff(got[f, :, :, 1:], db[f, :, :, 1:]) == 0
 
 
-@pytest.mark.parametrize("storage", ["f32", "f64", "f16"])
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16", "c16"])
 def test_reduce_conserved(capi, oracle_mod, storage):
     api, O = capi, oracle_mod
     dims = (24, 20, 18)
@@ -373,3 +375,67 @@ def test_errors_are_reported(capi):
     L = api.Lattice(5, 5, 5, api.F32, False, False)
     with pytest.raises(api.LbmError, match="velocity is not stored"):
         L.read(api.FIELD_VELOCITY)
+
+
+@pytest.mark.parametrize("size,nums,halo_mode", [((30, 20, 12), (2, 2, 1), 0), ((36, 24, 24), (3, 2, 2), 1),
+                                                 ((6, 8, 8), (2, 1, 1), 0), ((24, 24, 24), (4, 4, 4), 1),
+                                                 ((256, 64, 32), (2, 2, 1), 1)])
+def test_fused_x_exchange_equals_separate_launch(capi, size, nums, halo_mode):
+    """The x part of the exchange after alpha done by the one-cell alpha
+    kernel itself gives the same bits as its own copy launch: subdomains of
+    three cells in x (the x = 1 cells send both ways), 64 subdomains, the
+    benchmark's subdomain width."""
+    api = capi
+
+    def run(fused):
+        D = api.Domain(size, nums, api.F32, True, True)
+        D.set_params(api.Params.make(1.0 / 0.52, 0.52, api.les_coefficient(0.17), (0, 0, 0), 0.09))
+        D.set_halo_mode(halo_mode)
+        D.set_fused_exchange(fused)
+        D.reset()
+        D.perturb(SEED, 1e-2)
+        D.run(5, use_graph=False)
+        D.set_store_interval(0)
+        D.run(8, use_graph=True)
+        return [[L.read(f) for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY)] for L in D.subdomains]
+
+    for a, b in zip(run(True), run(False)):
+        for x, y in zip(a, b):
+            assert n_diff(x, y) == 0
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16", "c16"])
+def test_deviation_stats_match_the_stored_bits(capi, oracle_mod, storage):
+    """lbm_cu_deviation_stats against the oracle's stored bits (the two are
+    bit-identical): counts of zero, subnormal and saturated deviations over
+    the fluid cells, and the largest magnitude."""
+    api, O = capi, oracle_mod
+    dims = (32, 20, 16)
+    p = oracle_params(O, storage, dims, cs=0.17, u=0.1)
+    L = gpu_single(api, O, dims, storage, p, perturb=(SEED, 3e-2))
+    s = O.single(O.OracleKernels(storage), dims, p, storage)
+    s.k.perturb(s.lat, (0, 0, 0), dims, SEED, 3e-2)
+    for _ in range(5):
+        L.step(s.lat.counter & 1)
+        s.step()
+    got = api.deviation_stats(L)
+    raw = s.lat.dd[:, s.lat.flags == O.FLAG_FLUID]
+    b = raw.view(np.uint16).astype(np.int64)
+    ebits, mbits = {"f16": (5, 10), "bf16": (8, 7), "c16": (3, 12)}[storage]
+    e, m = (b >> mbits) & ((1 << ebits) - 1), b & ((1 << mbits) - 1)
+    top = (1 << ebits) - 1
+    sat = (b & 0x7fff) == (0x7fff if storage == "c16" else ((top << mbits) - 1))
+    if storage != "c16":
+        sat |= e == top
+    assert got["values"] == b.size
+    assert got["zero"] == int(((e == 0) & (m == 0)).sum())
+    assert got["subnormal"] == int(((e == 0) & (m != 0)).sum())
+    assert got["saturated"] == int(sat.sum())
+    if storage == "f16":
+        dev = raw.astype(np.float64)
+    elif storage == "bf16":
+        dev = (raw.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    else:
+        from test_oracle_pin import _c16_value
+        dev = _c16_value(raw)
+    assert got["max_abs"] == np.abs(dev).max()

@@ -228,21 +228,86 @@ def test_subgrid_collision_matches_formula(oracle_mod, storage, tol):
     assert rel.max() < tol
 
 
+def _c16_value(code):
+    """Value of c16 codes from the format's definition (float64): sign bit 15,
+    exponent e = bits 12-14, fraction m = bits 0-11; (1 + m/2^12) 2^(e-12)
+    for e > 0, m 2^-23 for e = 0."""
+    code = np.asarray(code, dtype=np.int64)
+    e, m = (code >> 12) & 7, (code & 0xfff).astype(np.float64)
+    mag = np.where(e > 0, (1.0 + m / 4096.0) * np.exp2(e - 12.0), m * 2.0 ** -23)
+    return np.where(code & 0x8000, -mag, mag)
+
+
+def _c16_code(v):
+    """c16 code of float32 values from the definition: |v| scaled by 2^-115
+    in float (so values below 2^-11 round once, to nearest even, to
+    multiples of 2^-34), then rounded to the nearest representable value,
+    halves away from zero, saturating at (2 - 2^-12) 2^-5."""
+    v = np.asarray(v, dtype=np.float32).astype(np.float64)
+    a = np.abs(v)
+    small = a < 2.0 ** -11
+    a = np.where(small, np.rint(a * 2.0 ** 34) * 2.0 ** -34, a)  # the float scaling's subnormal rounding
+    e = np.where(small, 0, np.floor(np.log2(np.maximum(a, 2.0 ** -11))) + 12).astype(np.int64)
+    step = np.where(small, 2.0 ** -23, np.exp2(e - 24.0))
+    q = np.floor(a / step + 0.5)  # halves away from zero (on the magnitude)
+    code = np.where(small, q, (e << 12) + (q - 4096)).astype(np.int64)  # a carry moves into the exponent
+    code = np.minimum(code, 0x7fff)
+    return (code | np.where(np.signbit(v), 0x8000, 0)).astype(np.uint16)
+
+
 def _stored_deviation(dd, storage):
     """The stored g_i = f_i - w_i of a shifted lattice, exactly, as float64."""
     if storage == "bf16":
         return (dd.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    if storage == "c16":
+        return _c16_value(dd)
     return dd.astype(np.float64)
 
 
 def _ulp16(x, storage):
-    """Spacing of the 16-bit type at x (half precision has subnormals below 2^-14)."""
-    mant, emin = (10, -14) if storage == "f16" else (7, -126)
+    """Spacing of the 16-bit type at x (half precision has subnormals below
+    2^-14, c16 below 2^-11)."""
+    mant, emin = {"f16": (10, -14), "bf16": (7, -126), "c16": (12, -11)}[storage]
     e = np.maximum(np.floor(np.log2(np.maximum(np.abs(x), 2.0 ** -140))), emin)
     return 2.0 ** (e - mant)
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def _c16_raw(oracle):
+    import ctypes as C
+
+    L = oracle.lib()
+    enc, dec = L.orc_c16_encode_raw, L.orc_c16_decode_raw
+    enc.argtypes = dec.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+    return enc, dec
+
+
+def test_c16_format_matches_its_definition(oracle_mod):
+    """The oracle's c16 encoder and decoder against the format's definition:
+    every one of the 65536 codes decodes to its value and encodes back to
+    itself (but -0); random values and exact halves between neighbours, in
+    and beyond the range, encode as the definition rounds them."""
+    import ctypes as C
+
+    enc, dec = _c16_raw(oracle_mod)
+    codes = np.arange(65536, dtype=np.uint16)
+    vals = np.empty(65536, np.float32)
+    dec(codes.ctypes.data_as(C.c_void_p), vals.ctypes.data_as(C.c_void_p), 65536)
+    assert np.array_equal(vals.astype(np.float64), _c16_value(codes))
+    back = np.empty(65536, np.uint16)
+    enc(vals.ctypes.data_as(C.c_void_p), back.ctypes.data_as(C.c_void_p), 65536)
+    keep = codes != 0x8000  # -0 encodes as -0 but +0 and -0 compare equal: skip the pair
+    assert np.array_equal(back[keep], codes[keep])
+    rng = np.random.default_rng(11)
+    x = np.concatenate([rng.uniform(-0.07, 0.07, 200000), rng.uniform(-1e-3, 1e-3, 100000),
+                        rng.uniform(-2e-6, 2e-6, 100000), [0.0625, -0.0625, 1.0, -5.0, 2.0 ** -11, 3 * 2.0 ** -24]])
+    mid = (_c16_value(codes[1:0x7fff]) + _c16_value(codes[2:0x8000])) / 2  # exact ties between neighbours
+    x = np.concatenate([x, mid[np.isfinite(mid)]]).astype(np.float32)
+    got = np.empty(x.size, np.uint16)
+    enc(x.ctypes.data_as(C.c_void_p), got.ctypes.data_as(C.c_void_p), x.size)
+    assert np.array_equal(got, _c16_code(x))
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16", "c16"])
 @pytest.mark.parametrize("cs", [0.0, 0.17])
 def test_deviation_form_collision_matches_formula(oracle_mod, storage, cs):
     """The shifted types collide on deviations with fused multiply-adds; the
@@ -317,7 +382,7 @@ def test_closed_box_conserves_mass(oracle_mod):
     assert abs(s.lat.dd.sum() - m0) / m0 < 2e-6
 
 
-@pytest.mark.parametrize("storage,tol", [("f16", 2e-2), ("bf16", 2e-1)])
+@pytest.mark.parametrize("storage,tol", [("f16", 2e-2), ("bf16", 2e-1), ("c16", 5e-3)])
 def test_shifted_storage_tracks_f64(oracle_mod, storage, tol):
     """Shifted half/bfloat16 storage against f64 over a short laminar run:
     relative error of the velocity field (RMS over fluid cells)."""

@@ -31,7 +31,8 @@ def _lattice(api, O, dims, storage, steps):
 
 
 @pytest.mark.parametrize("storage,dims,steps", [("f32", (48, 40, 36), 5), ("f64", (30, 26, 22), 4),
-                                                ("f16", (64, 64, 40), 3), ("bf16", (64, 48, 40), 3)])
+                                                ("f16", (64, 64, 40), 3), ("bf16", (64, 48, 40), 3),
+                                                ("c16", (32, 40, 24), 3)])
 def test_noalloc_sums_equal_allocating_sums(capi, oracle_mod, storage, dims, steps):
     api, O = capi, oracle_mod
     L = _lattice(api, O, dims, storage, steps)

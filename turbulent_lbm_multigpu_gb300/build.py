@@ -30,7 +30,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
            "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CU_SOURCES = ["lbm_capi.cu", "lbm_batch.cu", "lbm_io.cu"]
+CU_SOURCES = ["lbm_capi.cu", "lbm_batch.cu", "lbm_io.cu", "lbm_f64fma.cu"]
+# the contracted FP64 kernels: products may fuse into sums in this unit only
+FMAD_SOURCES = {"lbm_f64fma.cu"}
 
 
 def nvcc() -> str:
@@ -60,7 +62,8 @@ def build_lib(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src):
         obj = objdir / (Path(src).stem + ".o")
-        cmd = [nvcc()] + ARCH + NVFLAGS + ["-c", str(CSRC / src), "-o", str(obj)]
+        flags = [("-fmad=true" if f == "-fmad=false" and src in FMAD_SOURCES else f) for f in NVFLAGS]
+        cmd = [nvcc()] + ARCH + flags + ["-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         subprocess.run(cmd, check=True)

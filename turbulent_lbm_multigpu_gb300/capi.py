@@ -14,8 +14,8 @@ import numpy as np
 
 from .build import LIB
 
-F32, F64, F16, BF16 = 0, 1, 2, 3
-STORAGE_NAMES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16}
+F32, F64, F16, BF16, C16 = 0, 1, 2, 3, 4
+STORAGE_NAMES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16, "c16": C16}
 FIELD_DD, FIELD_VELOCITY, FIELD_DENSITY, FIELD_FLAGS = 0, 1, 2, 3
 FLAG_OBSTACLE, FLAG_FLUID, FLAG_VELOCITY_INJECTION, FLAG_GHOST_LAYER = 1, 2, 4, 8
 
@@ -86,12 +86,16 @@ def lib() -> C.CDLL:
         "lbm_cu_perturb": ([vp, ip, ip, u64, cd, vp], ci),
         "lbm_cu_step": ([vp, ci, vp], ci),
         "lbm_cu_set_kernel_shape": ([vp, ci], ci),
+        "lbm_cu_set_fp64_contraction": ([vp, ci], ci),
+        "lbm_cu_domain_set_fp64_contraction": ([vp, ci], ci),
+        "lbm_cu_domain_set_fused_exchange": ([vp, ci], ci),
         "lbm_cu_read": ([vp, ci, ip, ip, vp, vp], ci),
         "lbm_cu_write": ([vp, ci, ip, ip, vp, ip, vp], ci),
         "lbm_cu_halo": ([vp, ip, vp, ip, ip, ip, vp], ci),
         "lbm_cu_reduce_conserved": ([vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_reduce_conserved_noalloc": ([vp, ci, C.POINTER(cd), vp], ci),
         "lbm_cu_compare_velocity": ([vp, ci, vp, ci, C.POINTER(cd), vp], ci),
+        "lbm_cu_deviation_stats": ([vp, C.POINTER(cd), vp], ci),
         "lbm_cu_domain_create": ([ip, ip, ci, ci, ci, ci, C.POINTER(vp)], ci),
         "lbm_cu_domain_destroy": ([vp], ci),
         "lbm_cu_domain_wrap": ([C.POINTER(vp), ip, ip, ci, C.POINTER(vp)], ci),
@@ -199,6 +203,10 @@ class Lattice:
     def set_kernel_shape(self, cells_per_thread: int):
         check(lib().lbm_cu_set_kernel_shape(self.h, cells_per_thread))
 
+    def set_fp64_contraction(self, enable: bool):
+        """Double storage: fused multiply-adds in the step (1e-15 per step off the reference arithmetic)."""
+        check(lib().lbm_cu_set_fp64_contraction(self.h, int(enable)))
+
     def _shape(self, field, size):
         sx, sy, sz = size
         planes = {FIELD_DD: 19, FIELD_VELOCITY: 3, FIELD_DENSITY: 1, FIELD_FLAGS: 1}[field]
@@ -249,6 +257,15 @@ class Lattice:
         out = (C.c_double * 5)()
         check(lib().lbm_cu_reduce_conserved_noalloc(self.h, layout, out, stream))
         return np.array(out[:], dtype=np.float64)
+
+
+def deviation_stats(L: Lattice, stream=None):
+    """{values, zero, subnormal, saturated, max_abs} of a 16-bit lattice's stored deviations (fluid cells)."""
+    out = (C.c_double * 5)()
+    check(lib().lbm_cu_deviation_stats(L.h, out, stream))
+    n, z, sub, sat, mx = out[:]
+    return {"values": int(n), "zero": int(z), "subnormal": int(sub), "saturated": int(sat), "max_abs": mx,
+            "subnormal_fraction": sub / n if n else 0.0, "zero_fraction": z / n if n else 0.0}
 
 
 def compare_velocity(a: Lattice, layout_a: int, b: Lattice, layout_b: int, stream=None):
@@ -358,6 +375,13 @@ class Domain:
 
     def set_kernel_shape(self, cells_per_thread: int):
         check(lib().lbm_cu_domain_set_kernel_shape(self.h, cells_per_thread))
+
+    def set_fp64_contraction(self, enable: bool):
+        check(lib().lbm_cu_domain_set_fp64_contraction(self.h, int(enable)))
+
+    def set_fused_exchange(self, enable: bool):
+        """One-cell alpha steps do the x part of the exchange after them (default on)."""
+        check(lib().lbm_cu_domain_set_fused_exchange(self.h, int(enable)))
 
     def set_halo_mode(self, mode: int):
         """0: all 19 populations after alpha (reference); 1: the 5 read inward."""

@@ -50,6 +50,7 @@ int launch_tick(int storage, bool pair, bool les, const BatchArgs &a, int blocks
             case kF32: return launch_tick_t<float, true>(les, a, blocks, j, st);
             case kF16: return launch_tick_t<__half, true>(les, a, blocks, j, st);
             case kBF16: return launch_tick_t<__nv_bfloat16, true>(les, a, blocks, j, st);
+            case kC16: return launch_tick_t<c16_t, true>(les, a, blocks, j, st);
         }
         return fail("the two-cell kernels need a float arithmetic type");
     }
@@ -58,6 +59,7 @@ int launch_tick(int storage, bool pair, bool les, const BatchArgs &a, int blocks
         case kF64: return launch_tick_t<double, false>(les, a, blocks, j, st);
         case kF16: return launch_tick_t<__half, false>(les, a, blocks, j, st);
         case kBF16: return launch_tick_t<__nv_bfloat16, false>(les, a, blocks, j, st);
+        case kC16: return launch_tick_t<c16_t, false>(les, a, blocks, j, st);
     }
     return fail("unknown storage type");
 }
@@ -72,7 +74,7 @@ size_t cavity_bytes(const lbm_cavity &c, int store_v) {
 
 int check_cavity(const lbm_cavity &c) {
     if (c.nx < 3 || c.ny < 3 || c.nz < 3) return fail("cavity edges must be at least 3 cells");
-    if (c.storage < LBM_F32 || c.storage > LBM_BF16) return fail("unknown storage type");
+    if (c.storage < LBM_F32 || c.storage > LBM_C16) return fail("unknown storage type");
     if (!(c.tau0 > 0.5)) return fail("cavity tau0 must exceed 0.5");
     if (c.steps < 0) return fail("negative step count");
     return 0;
@@ -171,7 +173,8 @@ struct Ensemble {
             const Slot &s = slots[i];
             if (!s.active) continue;
             const bool pair = shape == 2 && s.spec.storage != LBM_F64 && !(s.spec.nx & 1);
-            const bool staged = shape == 3 && (s.spec.storage == LBM_F16 || s.spec.storage == LBM_BF16);
+            const bool staged =
+                shape == 3 && (s.spec.storage == LBM_F16 || s.spec.storage == LBM_BF16 || s.spec.storage == LBM_C16);
             const bool aligned = staged && ((int64_t)s.spec.nx * storage_bytes(s.spec.storage)) % 16 == 0;
             Group *g = nullptr;
             for (auto &x : groups)

@@ -48,7 +48,7 @@ int ensure_stage(lbm_lattice *l, size_t bytes) {
 
 // Parameters rounded to the arithmetic type R, plus the gravity chain
 // coefficients of lbm_alpha.cl:183-291 computed in R.
-template <typename R> void fill_params(const lbm_params &p, R out[16], int *grav) {
+template <typename R> void fill_params(const lbm_params &p, R out[P_COUNT], int *grav) {
     const R gx = (R)p.gravity[0], gy = (R)p.gravity[1], gz = (R)p.gravity[2];
     const R c18 = (R)(1.0f / 18.0f), c36 = (R)(1.0f / 36.0f);
     out[P_INV_TAU] = (R)p.inv_tau;
@@ -77,10 +77,10 @@ void set_params_desc(LatDesc &h, int storage, const lbm_params &p) {
     int grav = 0;
     if (storage == kF64) {
         fill_params<double>(p, h.pd, &grav);
-        for (int i = 0; i < 16; i++) h.pf[i] = (float)h.pd[i];
+        for (int i = 0; i < P_COUNT; i++) h.pf[i] = (float)h.pd[i];
     } else {
         fill_params<float>(p, h.pf, &grav);
-        for (int i = 0; i < 16; i++) h.pd[i] = (double)h.pf[i];
+        for (int i = 0; i < P_COUNT; i++) h.pd[i] = (double)h.pf[i];
     }
     h.grav = grav;
     h.gmode = p.gravity_mode ? 1 : 0;
@@ -382,6 +382,54 @@ __global__ void __launch_bounds__(kBlock) k_compare(LatDesc a, int la, LatDesc b
     if (threadIdx.x < 5) partial[blockIdx.x * 5 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// Classes of the stored 16-bit deviations (fluid cells, all 19 slots):
+// counts of all, zero, subnormal (nonzero below the format's smallest
+// normal magnitude) and saturated (the format's largest finite magnitude or
+// beyond) values, and the largest magnitude.  raw: the stored bits.
+template <typename S> struct DevClass;
+template <> struct DevClass<__half> {
+    __device__ static int of(uint16_t b) {
+        const uint32_t e = (b >> 10) & 31u, m = b & 1023u;
+        return e == 0 ? (m ? 2 : 1) : (e == 31 || (b & 0x7fffu) == 0x7bffu) ? 3 : 0;
+    }
+};
+template <> struct DevClass<__nv_bfloat16> {
+    __device__ static int of(uint16_t b) {
+        const uint32_t e = (b >> 7) & 255u, m = b & 127u;
+        return e == 0 ? (m ? 2 : 1) : (e == 255 || (b & 0x7fffu) == 0x7f7fu) ? 3 : 0;
+    }
+};
+template <> struct DevClass<c16_t> {
+    __device__ static int of(uint16_t b) {
+        const uint32_t e = (b >> 12) & 7u, m = b & 4095u;
+        return e == 0 ? (m ? 2 : 1) : (b & 0x7fffu) == 0x7fffu ? 3 : 0;
+    }
+};
+
+template <typename S>
+__global__ void __launch_bounds__(kBlock) k_dev_stats(LatDesc d, unsigned long long *count, unsigned int *maxbits) {
+    unsigned long long n[4] = {0, 0, 0, 0};
+    float mx = 0.0f;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < d.n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (d.flags[c] != kFluid) continue;
+#pragma unroll
+        for (int i = 0; i < 19; i++) {
+            const S *p = (const S *)d.dd + i * d.pstride + c;
+            n[0]++;
+            const int k = DevClass<S>::of(*(const uint16_t *)p);
+            if (k) n[k]++;
+            mx = fmaxf(mx, fabsf(Store<S>::dld(p)));
+        }
+    }
+    for (int q = 0; q < 4; q++) {
+        unsigned long long v = n[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&count[q], v);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(mx));  // non-negative floats order as integers
+}
+
 __global__ void k_compare_final(const double *partial, int nblocks, double *out) {
     if (threadIdx.x != 0) return;
     double r[5] = {0, 0, 0, 0, 0};
@@ -433,7 +481,7 @@ bool pair_shape(int storage, const LatDesc *tab, int ntab) {
 }
 
 int effective_shape(int storage, int shape, const LatDesc *tab, int ntab) {
-    if (shape == 0) shape = (storage == kF16 || storage == kBF16) ? 3 : 1;  // the measured best per storage
+    if (shape == 0) shape = (storage == kF16 || storage == kBF16 || storage == kC16) ? 3 : 1;  // the measured best per storage
     if (shape == 2 && pair_shape(storage, tab, ntab)) return 2;
     if (shape == 3 && storage != kF64) return 3;
     return 1;
@@ -446,6 +494,7 @@ static int launch_chunk(int storage, bool pair, int parity, bool les, const Doma
             case kF32: return launch_step_t<float, true>(parity, les, a, blocks, st);
             case kF16: return launch_step_t<__half, true>(parity, les, a, blocks, st);
             case kBF16: return launch_step_t<__nv_bfloat16, true>(parity, les, a, blocks, st);
+            case kC16: return launch_step_t<c16_t, true>(parity, les, a, blocks, st);
         }
         return fail("the two-cell kernels need a float arithmetic type");
     }
@@ -454,6 +503,7 @@ static int launch_chunk(int storage, bool pair, int parity, bool les, const Doma
         case kF64: return launch_step_t<double, false>(parity, les, a, blocks, st);
         case kF16: return launch_step_t<__half, false>(parity, les, a, blocks, st);
         case kBF16: return launch_step_t<__nv_bfloat16, false>(parity, les, a, blocks, st);
+        case kC16: return launch_step_t<c16_t, false>(parity, les, a, blocks, st);
     }
     return fail("unknown storage type");
 }
@@ -471,8 +521,8 @@ static int sm_count() {
     return cache[dev];
 }
 
-template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
-static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
+template <typename S, bool LES, bool BETA, bool ONE, int N, bool W32>
+static int launch_staged_w(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     // the ring exceeds the default 48 KB of dynamic shared memory; the limit
     // is raised once per device
     static bool attr[64] = {};
@@ -480,14 +530,27 @@ static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     CU(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail("device index out of range");
     if (!attr[dev]) {
-        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N, W32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 Tile<S>::SMEM));
         attr[dev] = true;
     }
     const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
-    k_step_staged<S, LES, BETA, ONE, N><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
+    k_step_staged<S, LES, BETA, ONE, N, W32><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
     CU(cudaGetLastError());
     return 0;
+}
+
+// Beta steps whose lattices all span fewer than 2^32 population elements
+// form their scatter addresses in 32-bit arithmetic (scatter_ptr).
+template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
+static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
+    if constexpr (BETA) {
+        bool w32 = true;
+        for (int i = 0; i < a.ntab; i++)
+            if (19 * a.tab[i].pstride >= ((int64_t)1 << 32)) w32 = false;
+        if (w32) return launch_staged_w<S, LES, BETA, ONE, N, true>(a, tiles, st);
+    }
+    return launch_staged_w<S, LES, BETA, ONE, N, false>(a, tiles, st);
 }
 
 template <typename S, bool LES, bool BETA>
@@ -508,6 +571,7 @@ int staged_cells(int storage) {
         case kF32: return Tile<float>::T;
         case kF16: return Tile<__half>::T;
         case kBF16: return Tile<__nv_bfloat16>::T;
+        case kC16: return Tile<c16_t>::T;
     }
     return 0;
 }
@@ -527,6 +591,7 @@ int launch_staged_batch(int storage, bool beta, bool les, const BatchArgs &a, in
         case kF32: return launch_staged_batch_t<float>(beta, les, a, tiles, st);
         case kF16: return launch_staged_batch_t<__half>(beta, les, a, tiles, st);
         case kBF16: return launch_staged_batch_t<__nv_bfloat16>(beta, les, a, tiles, st);
+        case kC16: return launch_staged_batch_t<c16_t>(beta, les, a, tiles, st);
     }
     return fail("the staged kernels take float, half or bfloat16 storage");
 }
@@ -555,11 +620,14 @@ int launch_step(int storage, int shape, int parity, bool les, const LatDesc *hta
             units += a.tab[i].nblocks;
         }
         int rc;
-        if (staged) {
+        if (shape == kShapeF64Fma && storage == kF64) {
+            rc = launch_step_f64_fma(parity, les, a, units, st);
+        } else if (staged) {
             switch (storage) {
                 case kF32: rc = launch_staged_t<float>(parity, les, a, units, st); break;
                 case kF16: rc = launch_staged_t<__half>(parity, les, a, units, st); break;
-                default: rc = launch_staged_t<__nv_bfloat16>(parity, les, a, units, st); break;
+                case kBF16: rc = launch_staged_t<__nv_bfloat16>(parity, les, a, units, st); break;
+                default: rc = launch_staged_t<c16_t>(parity, les, a, units, st); break;
             }
         } else {
             rc = launch_chunk(storage, pair, parity, les, a, units, st);
@@ -681,7 +749,7 @@ int lbm_cu_create(int nx, int ny, int nz, int storage, int store_velocity, int s
     if (!out) return fail("out is NULL");
     *out = nullptr;
     if (nx < 3 || ny < 3 || nz < 3) return fail("each lattice dimension must be at least 3");
-    if (storage < kF32 || storage > kBF16) return fail("unknown storage type");
+    if (storage < kF32 || storage > kC16) return fail("unknown storage type");
     const int64_t n = (int64_t)nx * ny * nz;
     if (n > ((int64_t)1 << 31) - 1) return fail("lattice has more than 2^31-1 cells");
     lbm_lattice *l = new lbm_lattice();
@@ -755,6 +823,7 @@ int lbm_cu_init(lbm_lattice *l, const int bc[6], void *stream) {
         case kF64: k_init<double><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
         case kF16: k_init<__half><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
         case kBF16: k_init<__nv_bfloat16><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
+        case kC16: k_init<c16_t><<<g, kBlock, 0, S(stream)>>>(l->h, bc[0], bc[1], bc[2], bc[3], bc[4], bc[5], l->store_v, l->store_rho); break;
     }
     CU(cudaGetLastError());
     return 0;
@@ -769,6 +838,7 @@ int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t see
         case kF64: PERT(double); break;
         case kF16: PERT(__half); break;
         case kBF16: PERT(__nv_bfloat16); break;
+        case kC16: PERT(c16_t); break;
     }
 #undef PERT
     CU(cudaGetLastError());
@@ -778,7 +848,8 @@ int lbm_cu_perturb(lbm_lattice *l, const int o[3], const int ph[3], uint64_t see
 int lbm_cu_step(lbm_lattice *l, int parity, void *stream) {
     if (!l) return fail("NULL lattice");
     const LatDesc &h = l->h;
-    return launch_step(l->storage, effective_shape(l->storage, l->shape, &h, 1), parity & 1, uses_les(h), &h, 1,
+    const int shape = l->fma64 && l->storage == kF64 ? kShapeF64Fma : effective_shape(l->storage, l->shape, &h, 1);
+    return launch_step(l->storage, shape, parity & 1, uses_les(h), &h, 1,
                        l->store_v, l->store_rho, S(stream));
 }
 
@@ -848,6 +919,7 @@ static int box_io(lbm_lattice *l, int field, const int o[3], const int s[3], voi
             case kF64: BOX(double, double); break;
             case kF16: BOX(__half, float); break;
             case kBF16: BOX(__nv_bfloat16, float); break;
+            case kC16: BOX(c16_t, float); break;
         }
 #undef BOX
     } else if (field == LBM_FIELD_FLAGS) {
@@ -925,6 +997,7 @@ int lbm_cu_reduce_conserved(lbm_lattice *l, int layout, double out[5], void *str
         case kF64: k_reduce<double><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
         case kF16: k_reduce<__half><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
         case kBF16: k_reduce<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kC16: k_reduce<c16_t><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
     }
     CU(cudaGetLastError());
     k_reduce_final<<<1, 32, 0, st>>>(partial, blocks, res);
@@ -951,12 +1024,14 @@ int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int la
         case kF64: CMP(SA_, double); break;         \
         case kF16: CMP(SA_, __half); break;         \
         case kBF16: CMP(SA_, __nv_bfloat16); break; \
+        case kC16: CMP(SA_, c16_t); break;          \
     }
     switch (a->storage) {
         case kF32: CMPB(float); break;
         case kF64: CMPB(double); break;
         case kF16: CMPB(__half); break;
         case kBF16: CMPB(__nv_bfloat16); break;
+        case kC16: CMPB(c16_t); break;
     }
 #undef CMPB
 #undef CMP
@@ -965,6 +1040,34 @@ int lbm_cu_compare_velocity(lbm_lattice *a, int layout_a, lbm_lattice *b, int la
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(out, res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int lbm_cu_deviation_stats(lbm_lattice *l, double out[5], void *stream) {
+    if (!l || !out) return fail("NULL argument");
+    if (l->storage != kF16 && l->storage != kBF16 && l->storage != kC16)
+        return fail("deviation statistics exist for the 16-bit storage types");
+    if (ensure_stage(l, 64)) return -1;
+    unsigned long long *cnt = (unsigned long long *)l->stage;
+    unsigned int *mx = (unsigned int *)(cnt + 4);
+    cudaStream_t st = S(stream);
+    CU(cudaMemsetAsync(l->stage, 0, 64, st));
+    const int blocks = std::min<int64_t>(kRedBlocks, std::max<int64_t>(1, grid_for(l->n)));
+    switch (l->storage) {
+        case kF16: k_dev_stats<__half><<<blocks, kBlock, 0, st>>>(l->h, cnt, mx); break;
+        case kBF16: k_dev_stats<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, cnt, mx); break;
+        default: k_dev_stats<c16_t><<<blocks, kBlock, 0, st>>>(l->h, cnt, mx); break;
+    }
+    CU(cudaGetLastError());
+    unsigned long long h[4];
+    unsigned int hm = 0;
+    CU(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&hm, mx, sizeof(hm), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    float m;
+    memcpy(&m, &hm, 4);
+    for (int q = 0; q < 4; q++) out[q] = (double)h[q];
+    out[4] = m;
     return 0;
 }
 
@@ -1042,6 +1145,7 @@ extern "C" int lbm_cu_reduce_conserved_noalloc(lbm_lattice *l, int layout, doubl
         case kF64: k_reduce<double><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
         case kF16: k_reduce<__half><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
         case kBF16: k_reduce<__nv_bfloat16><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
+        case kC16: k_reduce<c16_t><<<blocks, kBlock, 0, st>>>(l->h, layout & 1, partial); break;
     }
     CU(cudaGetLastError());
     k_reduce_final_warps<<<1, 160, 0, st>>>(partial, blocks, res);
@@ -1069,12 +1173,15 @@ struct lbm_domain {
     std::vector<LatDesc> h_tab;  // descriptors of the subdomains
     int shape = 0;               // requested kernel shape (0: per storage type)
     int eff_shape = 1;           // the shape the subdomains run
+    int fma64 = 0;               // double storage: contracted FP64 kernels
     bool tab_dirty = true;
     // halo plans [0 = after beta, 1 = after alpha][axis]
     std::vector<HaloDesc> plan[2][3];
     int64_t plan_cells[2][3] = {};
     int plan_planes[2][3] = {};
     int halo_mode = 0;  // 0: all 19 populations after alpha (reference), 1: the 5 read inward
+    bool fuse_x = true;    // let one-cell alpha steps do the x part of the exchange after them
+    bool x_fused = false;  // ... and they do, for the current kernel shape (domain_upload_tab)
     int64_t counter = 0;
     int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
     cudaGraphExec_t graph = nullptr;
@@ -1135,6 +1242,38 @@ int domain_geometry(lbm_domain *D);
 
 void drop_graph(lbm_domain *D);
 
+// The x part of the exchange after alpha steps, moved into the one-cell
+// alpha kernel: each sender's descriptor gets its x neighbours' population
+// planes and the planes to copy (those of the x plan after alpha).
+void domain_fuse_x(lbm_domain *D, std::vector<LatDesc> &t, int eff_shape) {
+    const bool fuse = D->fuse_x && eff_shape == 1 && !D->plan[1][0].empty();
+    for (auto &d : t) {
+        d.xhi = d.xlo = nullptr;
+        d.xmask_hi = d.xmask_lo = 0;
+        d.xdiv_m = d.xdiv_s1 = d.xdiv_s2 = 0;
+    }
+    if (!fuse) return;
+    for (const HaloDesc &h : D->plan[1][0]) {
+        size_t a = 0;
+        while (a < D->subs.size() && D->subs[a]->dd != h.src) a++;
+        if (a == D->subs.size()) continue;
+        LatDesc &d = t[a];
+        uint32_t mask = 0;
+        for (int k = 0; k < h.pl.n; k++) mask |= 1u << h.pl.f[k];
+        if (h.db.ox == 0) {  // the receiver's ghost layer x = 0: the +x neighbour, sent from x = nx - 2
+            d.xhi = h.dst;
+            d.xmask_hi = mask;
+        } else {  // x = nx - 1 of the -x neighbour, sent from x = 1
+            d.xlo = h.dst;
+            d.xmask_lo = mask;
+        }
+        const FastDiv fd = FastDiv::make((uint32_t)d.nx);
+        d.xdiv_m = fd.m;
+        d.xdiv_s1 = fd.s1;
+        d.xdiv_s2 = fd.s2;
+    }
+}
+
 int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
     (void)st;
     if (!D->tab_dirty && D->owns) return 0;
@@ -1142,12 +1281,16 @@ int domain_upload_tab(lbm_domain *D, cudaStream_t st) {
     // compare, and drop a graph captured with the old descriptors
     std::vector<LatDesc> t;
     for (auto *l : D->subs) t.push_back(l->h);
+    const int eff = D->fma64 && D->storage == kF64 ? kShapeF64Fma
+                                                   : effective_shape(D->storage, D->shape, t.data(), (int)t.size());
+    domain_fuse_x(D, t, eff);
     if (!D->tab_dirty && t.size() == D->h_tab.size() &&
         memcmp(t.data(), D->h_tab.data(), t.size() * sizeof(LatDesc)) == 0)
         return 0;
     drop_graph(D);
     D->h_tab.swap(t);
-    D->eff_shape = effective_shape(D->storage, D->shape, D->h_tab.data(), (int)D->h_tab.size());
+    D->eff_shape = eff;
+    D->x_fused = D->fuse_x && eff == 1 && !D->plan[1][0].empty();
     D->tab_dirty = false;
     return 0;
 }
@@ -1172,7 +1315,7 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
         return -1;
     if (timed && domain_record(D, st, &e1)) return -1;
     for (int a = 0; a < 3; a++)
-        if (!D->plan[parity][a].empty() &&
+        if (!D->plan[parity][a].empty() && !(parity == 1 && a == 0 && D->x_fused) &&
             launch_halo_batch(D->storage, D->plan[parity][a].data(), (int)D->plan[parity][a].size(), D->plan_cells[parity][a],
                               D->plan_planes[parity][a], st))
             return -1;
@@ -1437,13 +1580,38 @@ int lbm_cu_domain_set_kernel_shape(lbm_domain *D, int cells_per_thread) {
     return 0;
 }
 
+int lbm_cu_set_fp64_contraction(lbm_lattice *l, int enable) {
+    if (!l) return fail("NULL lattice");
+    if (l->storage != kF64) return fail("contracted kernels exist for double storage only");
+    l->fma64 = enable ? 1 : 0;
+    return 0;
+}
+
+int lbm_cu_domain_set_fp64_contraction(lbm_domain *D, int enable) {
+    if (!D) return fail("NULL domain");
+    if (D->storage != kF64) return fail("contracted kernels exist for double storage only");
+    D->fma64 = enable ? 1 : 0;
+    D->tab_dirty = true;
+    drop_graph(D);
+    return 0;
+}
+
 int lbm_cu_domain_set_halo_mode(lbm_domain *D, int mode) {
     if (!D) return fail("NULL domain");
     if (mode != 0 && mode != 1) return fail("halo mode is 0 (all populations) or 1 (inward populations)");
     if (mode == D->halo_mode) return 0;
     D->halo_mode = mode;
     drop_graph(D);
+    D->tab_dirty = true;  // the fused x copies take their planes from the plans
     return domain_build_plans(D);
+}
+
+int lbm_cu_domain_set_fused_exchange(lbm_domain *D, int enable) {
+    if (!D) return fail("NULL domain");
+    D->fuse_x = enable != 0;
+    D->tab_dirty = true;
+    drop_graph(D);
+    return 0;
 }
 
 int lbm_cu_domain_profile(lbm_domain *D, int enable) {

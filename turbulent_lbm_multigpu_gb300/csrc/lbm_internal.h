@@ -47,6 +47,14 @@ inline int cells_per_block(bool pair) { return pair ? kPairCells : kBlock; }
 // 3 float/half/bfloat16 storage; otherwise 1.
 int effective_shape(int storage, int shape, const LatDesc *tab, int ntab);
 
+// Internal kernel shape of double lattices that run the contracted FP64
+// kernels (lbm_cu_set_fp64_contraction): one cell per thread, fused
+// multiply-adds (lbm_f64fma.cu).
+constexpr int kShapeF64Fma = 4;
+// One step of up to kParamLattices double lattices with the contracted
+// kernels (lbm_f64fma.cu); blocks of kBlock cells.
+int launch_step_f64_fma(int parity, bool les, const DomainArgs &a, int blocks, cudaStream_t st);
+
 // One step over `ntab` lattices of one storage type, kParamLattices
 // descriptors per launch.
 int launch_step(int storage, int shape, int parity, bool les, const LatDesc *htab, int ntab, int sv, int sr,
@@ -78,4 +86,5 @@ struct lbm_lattice {
     void *stage = nullptr;  // staging for host copies and reduction partials
     size_t stage_bytes = 0;
     int shape = 0;  // requested kernel shape (0: per storage type, see effective_shape)
+    int fma64 = 0;  // double storage: contracted FP64 kernels (lbm_cu_set_fp64_contraction)
 };

@@ -35,11 +35,14 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <type_traits>
 
 namespace lbm {
 
 enum : uint8_t { kObstacle = 1, kFluid = 2, kLid = 4, kGhost = 8 };
-enum Storage : int { kF32 = 0, kF64 = 1, kF16 = 2, kBF16 = 3 };
+enum Storage : int { kF32 = 0, kF64 = 1, kF16 = 2, kBF16 = 3, kC16 = 4 };
 
 // D3Q19 directions in reference order (src/main.cpp:38-66).
 __host__ __device__ constexpr int dir_x(int i) {
@@ -168,6 +171,59 @@ template <> struct Store<__nv_bfloat16> {
     }
 };
 
+// c16: a 16-bit float of this project for the shifted deviations g = f - w,
+// with more significand and less range than binary16 (whose five exponent
+// bits span magnitudes the deviations never reach): 1 sign bit, 3 exponent
+// bits e, 12 fraction bits m;
+//   e = 1..7: |g| = (1 + m / 2^12) 2^(e - 12)   (binades 2^-11 .. 2^-4),
+//   e = 0:    |g| = m 2^-23                      (subnormal),
+// so |g| < 2^-4 (|f_i - w_i| < 1/16, flows up to |u| ~ 0.28) with a 13-bit
+// significand: 4x finer than binary16's 11 bits.  The format is float's
+// bit layout with the exponent range moved down by 115 binades: scaling by
+// 2^-115 maps the format's subnormal range onto float's subnormals, so
+// float's own subnormal rounding and bit layout do most of the work.
+// Encoding: |g| 2^-115 (one float rounding, which only values in the
+// subnormal range undergo), then the fraction rounded to 12 bits, halves
+// away from zero; magnitudes beyond the largest value (2 - 2^-12) 2^-5
+// saturate to it.  Decoding is exact.  The CPU oracle states the same steps.
+struct c16_t {
+    uint16_t bits;
+};
+__host__ __device__ __forceinline__ uint32_t c16_encode(float v) {
+    const float x = fabsf(v) * 0x1p-115f;
+    uint32_t a, u;
+    memcpy(&a, &x, 4);
+    memcpy(&u, &v, 4);
+    const uint32_t r = (a + 0x400u) >> 11;
+    return ((u >> 16) & 0x8000u) | (r < 0x7fffu ? r : 0x7fffu);
+}
+// The code in the upper half of a 32-bit word (the lower half is ignored).
+__host__ __device__ __forceinline__ float c16_decode_hi(uint32_t w) {
+    const uint32_t u = (uint32_t)((int32_t)w >> 5) & 0x83fff800u;
+    float x;
+    memcpy(&x, &u, 4);
+    return x * 0x1p115f;  // exact, subnormal x included
+}
+__host__ __device__ __forceinline__ float c16_decode(uint32_t c) { return c16_decode_hi(c << 16); }
+template <> struct Store<c16_t> {
+    using R = float;
+    static constexpr bool kDev = true;
+    __device__ static __forceinline__ R dld(const c16_t *p) { return c16_decode(p->bits); }
+    __device__ static __forceinline__ void dst(c16_t *p, R v) { p->bits = (uint16_t)c16_encode(v); }
+    __device__ static __forceinline__ P2 dld2(const c16_t *p) {
+        const uint32_t w = *(const uint32_t *)p;
+        return P2{c16_decode(w), c16_decode_hi(w)};
+    }
+    __device__ static __forceinline__ void dst2(c16_t *p, P2 v) {
+        *(uint32_t *)p = c16_encode(v.x) | (c16_encode(v.y) << 16);
+    }
+    __device__ static __forceinline__ uint32_t dbits(R v) { return c16_encode(v); }
+    __device__ static __forceinline__ R ld(const c16_t *p, R w) { return c16_decode(p->bits) + w; }
+    __device__ static __forceinline__ void st(c16_t *p, R v, R w) { p->bits = (uint16_t)c16_encode(v - w); }
+    __device__ static __forceinline__ P2 ld2(const c16_t *p, R w) { return dld2(p) + P2{w, w}; }
+    __device__ static __forceinline__ void st2(c16_t *p, P2 v, R w) { dst2(p, v - P2{w, w}); }
+};
+
 // Constants exactly as the reference writes them: (T)(float literal).
 template <typename R> struct K {
     static constexpr R c18 = (R)(1.0f / 18.0f);
@@ -220,10 +276,20 @@ struct LatDesc {
     int32_t grav;         // gravity terms non-zero (alpha kernel)
     int32_t gmode;        // 0: the reference's chained terms, 1: per-term forcing
     int32_t parity;       // step counter parity at the start of a batch tick
-    double pd[16];        // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
-    float pf[16];
+    // Subdomains of a domain whose one-cell alpha steps also do the x part of
+    // the exchange that follows them (CController::syncAlpha,
+    // src/CController.hpp:265-320): after its own update, the thread of a
+    // cell at x = nx-2 copies the planes in xmask_hi of that cell into the
+    // ghost cell x = 0 of the +x neighbour (population planes xhi), a cell at
+    // x = 1 the planes in xmask_lo into x = nx-1 of the -x neighbour (xlo).
+    // Null: no such neighbour (or the exchange runs as its own launch).
+    void *xhi, *xlo;
+    uint32_t xmask_hi, xmask_lo;
+    uint32_t xdiv_m, xdiv_s1, xdiv_s2;  // c / nx by multiply and shifts
+    double pd[13];        // inv_tau, tau0, les_c, lid, k0..k8 (gravity chain)
+    float pf[13];
 };
-enum { P_INV_TAU = 0, P_TAU0 = 1, P_LES = 2, P_LID = 3, P_K0 = 4 };
+enum { P_INV_TAU = 0, P_TAU0 = 1, P_LES = 2, P_LID = 3, P_K0 = 4, P_COUNT = 13 };
 
 template <typename R> __device__ __forceinline__ R par(const LatDesc &d, int i);
 template <> __device__ __forceinline__ float par<float>(const LatDesc &d, int i) { return d.pf[i]; }
@@ -439,23 +505,26 @@ __device__ __forceinline__ void beta_case(int fl, M f[19], M &r, M &vx, M &vy, M
 }
 
 // The alpha kernel's flag switch (lbm_alpha.cl:177-484): returns whether the
-// cell writes its populations (fluid and lid, gravity terms applied).
+// cell writes its populations (fluid and lid, gravity terms applied).  The
+// gravity terms (and the density they leave, lbm_alpha.cl:173) are computed
+// only when there is gravity or the density is stored (need_rho).
 template <typename M, bool LES>
-__device__ __forceinline__ bool alpha_case(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+__device__ __forceinline__ bool alpha_case(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d,
+                                           bool need_rho) {
     using R = typename Scalar<M>::T;
     M t[9];
     if (fl == kFluid) {
         const M v2 = (vx * vx + vy * vy) + vz * vz;
         const M dp = r - Bc<M>::of(K<R>::k15) * v2;
         collide<M, LES>(f, r, vx, vy, vz, dp, d);
-        r = gravity_chain<M>(r, d, t);
+        if (d.grav || need_rho) r = gravity_chain<M>(r, d, t);
     } else if (fl == kLid) {
         vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
         r = Bc<M>::of((R)1.0f);
         const M v2 = (vx * vx + vy * vy) + vz * vz;
         const M dp = r - Bc<M>::of(K<R>::k15) * v2;
         equilibria<M>(vx, vy, vz, dp, f);
-        r = gravity_chain<M>(r, d, t);
+        if (d.grav || need_rho) r = gravity_chain<M>(r, d, t);
     } else {
         if (fl == kObstacle) {  // lbm_alpha.cl:305-343, populations untouched
             vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
@@ -482,9 +551,10 @@ __device__ __forceinline__ bool alpha_case(int fl, M f[19], M &r, M &vx, M &vy, 
 //   A = dd_param - 1 = (rho - 1) - 3/2 |u|^2  (u = j, as in the reference),
 //   f_i^eq - w_i = w_i (A + 3 e_i.u + 9/2 (e_i.u)^2),
 //   g_i' = (1 - omega) g_i + omega (f_i^eq - w_i),
-// taken per opposite pair (2k, 2k+1) as P +- Q with P = omega w (A + 9/2 s^2),
-// Q = 3 omega w s, s = e_2k . u.  kCW and kCP are the float weights' exact
-// offsets: sum_i w_i - 1 = 2^-26 and sum_i e_ix^2 w_i - (float)(1/3) = -2^-27.
+// taken per opposite pair (2k, 2k+1) as P +- Q with P = omega w A +
+// (9/2 omega w s) s, Q = 3 omega w s, s = e_2k . u, and Q folded into the
+// last multiply-add of each population.  kCW and kCP are the float weights'
+// exact offsets: sum_i w_i - 1 = 2^-26 and sum_i e_ix^2 w_i - (float)(1/3) = -2^-27.
 constexpr float kCW = 0x1p-26f;
 constexpr float kCP = -0x1p-27f;
 
@@ -511,13 +581,13 @@ __device__ __forceinline__ void dev_moments(const M g[19], M &dl, M &jx, M &jy, 
     m2[5] = s[6] - s[7];
 }
 
-// One opposite pair: g_2k' = (1-omega) g_2k + P + Q, g_2k+1' = ... + P - Q.
+// One opposite pair: g_2k' = (1-omega) g_2k + P + Q, g_2k+1' = ... + P - Q,
+// P = aA + (a45 v) v, Q = b v (six operations).
 template <typename M>
-__device__ __forceinline__ void dev_pair(M g[19], int k, M v, M a, M b, M A, M om1) {
-    const M h = mfma(Bc<M>::of(K<float>::k45) * v, v, A);
-    const M P = a * h, Q = b * v;
-    g[2 * k] = mfma(om1, g[2 * k], P + Q);
-    g[2 * k + 1] = mfma(om1, g[2 * k + 1], P - Q);
+__device__ __forceinline__ void dev_pair(M g[19], int k, M v, M aA, M a45, M b, M om1) {
+    const M P = mfma(a45 * v, v, aA);
+    g[2 * k] = mfma(b, v, mfma(om1, g[2 * k], P));
+    g[2 * k + 1] = mfma(-b, v, mfma(om1, g[2 * k + 1], P));
 }
 
 // Relaxation of all 19 deviations with rate om towards the equilibrium of
@@ -528,15 +598,17 @@ __device__ __forceinline__ void dev_relax(M g[19], M om, M A, M vx, M vy, M vz) 
     const M a18 = om * Bc<M>::of(K<float>::c18), a36 = om * Bc<M>::of(K<float>::c36);
     const M a3 = om * Bc<M>::of(K<float>::c3);
     const M b18 = Bc<M>::of(K<float>::k3) * a18, b36 = Bc<M>::of(K<float>::k3) * a36;
-    dev_pair(g, 0, vx, a18, b18, A, om1);
-    dev_pair(g, 1, vy, a18, b18, A, om1);
-    dev_pair(g, 2, vx + vy, a36, b36, A, om1);
-    dev_pair(g, 3, vx - vy, a36, b36, A, om1);
-    dev_pair(g, 4, vx + vz, a36, b36, A, om1);
-    dev_pair(g, 5, vx - vz, a36, b36, A, om1);
-    dev_pair(g, 6, vy + vz, a36, b36, A, om1);
-    dev_pair(g, 7, vy - vz, a36, b36, A, om1);
-    dev_pair(g, 8, vz, a18, b18, A, om1);
+    const M aA18 = a18 * A, aA36 = a36 * A;
+    const M h18 = Bc<M>::of(K<float>::k45) * a18, h36 = Bc<M>::of(K<float>::k45) * a36;
+    dev_pair(g, 0, vx, aA18, h18, b18, om1);
+    dev_pair(g, 1, vy, aA18, h18, b18, om1);
+    dev_pair(g, 2, vx + vy, aA36, h36, b36, om1);
+    dev_pair(g, 3, vx - vy, aA36, h36, b36, om1);
+    dev_pair(g, 4, vx + vz, aA36, h36, b36, om1);
+    dev_pair(g, 5, vx - vz, aA36, h36, b36, om1);
+    dev_pair(g, 6, vy + vz, aA36, h36, b36, om1);
+    dev_pair(g, 7, vy - vz, aA36, h36, b36, om1);
+    dev_pair(g, 8, vz, aA18, h18, b18, om1);
     g[18] = mfma(om1, g[18], a3 * A);
 }
 
@@ -617,19 +689,20 @@ __device__ __forceinline__ void dev_beta(int fl, M g[19], M &r, M &vx, M &vy, M 
 
 // The alpha kernel's flag switch (as alpha_case) in deviation form.
 template <typename M, bool LES>
-__device__ __forceinline__ bool dev_alpha(int fl, M g[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+__device__ __forceinline__ bool dev_alpha(int fl, M g[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d,
+                                          bool need_rho) {
     M dl, m2[6], t[9];
     dev_moments<M>(g, dl, vx, vy, vz, m2);
     r = Bc<M>::of(1.0f) + dl;
     if (fl == kFluid) {
         const M A = dev_dp1(vx, vy, vz, dl);
         dev_collide<M, LES>(g, dl, vx, vy, vz, m2, A, d);
-        r = gravity_chain<M>(r, d, t);
+        if (d.grav || need_rho) r = gravity_chain<M>(r, d, t);
     } else if (fl == kLid) {
         vx = parm<M>(d, P_LID); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
         const M A = Bc<M>::of(-K<float>::k15) * (vx * vx);
         dev_equilibria<M>(vx, vy, vz, A, g);
-        r = gravity_chain<M>(Bc<M>::of(1.0f), d, t);
+        if (d.grav || need_rho) r = gravity_chain<M>(Bc<M>::of(1.0f), d, t);
     } else {
         if (fl == kObstacle) {
             vx = Bc<M>::of(0); vy = Bc<M>::of(0); vz = Bc<M>::of(0);
@@ -657,12 +730,13 @@ __device__ __forceinline__ void beta_phys(int fl, M f[19], M &r, M &vx, M &vy, M
     }
 }
 template <typename M, bool LES, bool DEV>
-__device__ __forceinline__ bool alpha_phys(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d) {
+__device__ __forceinline__ bool alpha_phys(int fl, M f[19], M &r, M &vx, M &vy, M &vz, const LatDesc &d,
+                                           bool need_rho) {
     if constexpr (DEV) {
-        return dev_alpha<M, LES>(fl, f, r, vx, vy, vz, d);
+        return dev_alpha<M, LES>(fl, f, r, vx, vy, vz, d, need_rho);
     } else {
         moments_alpha<M>(f, r, vx, vy, vz);
-        return alpha_case<M, LES>(fl, f, r, vx, vy, vz, d);
+        return alpha_case<M, LES>(fl, f, r, vx, vy, vz, d, need_rho);
     }
 }
 
@@ -736,21 +810,69 @@ __global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_beta(const __gr
         beta_cell<S, LES, false>(d, c, a.store_v, a.store_rho);
 }
 
+// Exact quotient of a 32-bit n by an invariant divisor from its multiplier
+// and shifts (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, figure 4.1).
+__device__ __forceinline__ uint32_t div_invariant(uint32_t n, uint32_t m, uint32_t s1, uint32_t s2) {
+    const uint32_t t = __umulhi(m, n);
+    return (t + ((n - t) >> s1)) >> s2;
+}
+
+// The x part of the exchange after an alpha step, done by the cells that
+// send it (see LatDesc::xhi): which way(s) cell c sends, bit 0 towards +x
+// (c at x = nx - 2), bit 1 towards -x (x = 1).  The receiving ghost cells
+// are not touched by their own lattice's alpha step (lbm_alpha.cl:31-32),
+// and the y and z parts run after the launch, so the corners still travel
+// in two hops.
+__device__ __forceinline__ int alpha_push_dirs(const LatDesc &d, int64_t c) {
+    if (!d.xhi && !d.xlo) return 0;
+    const uint32_t cc = (uint32_t)c, nx = (uint32_t)d.nx;
+    const uint32_t x = cc - div_invariant(cc, d.xdiv_m, d.xdiv_s1, d.xdiv_s2) * nx;
+    return (d.xhi && x == nx - 2 ? 1 : 0) | (d.xlo && x == 1 ? 2 : 0);
+}
+
+// Slot f of cell c after its alpha step is v(f); copy the selected slots to
+// the neighbours' ghost cells (the same conversion as the cell's own stores,
+// so the bits are those a copy of the slots would move).
+template <typename S, typename V>
+__device__ __forceinline__ void alpha_push(const LatDesc &d, int64_t c, int dirs, V v) {
+    const int64_t ps = d.pstride, sh = (int64_t)d.nx - 2;
+    if (dirs & 1) {
+        S *dst = (S *)d.xhi + (c - sh);
+#pragma unroll
+        for (int f = 0; f < 19; f++)
+            if (d.xmask_hi & (1u << f)) pop_st<S>(dst + f * ps, v(f), f);
+    }
+    if (dirs & 2) {
+        S *dst = (S *)d.xlo + (c + sh);
+#pragma unroll
+        for (int f = 0; f < 19; f++)
+            if (d.xmask_lo & (1u << f)) pop_st<S>(dst + f * ps, v(f), f);
+    }
+}
+
 template <typename S, bool LES>
 __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int store_v, int store_rho) {
     using R = typename Store<S>::R;
     const int fl = d.flags[c];
-    if (fl == kGhost) return;  // lbm_alpha.cl:31-32
+    const int dirs = alpha_push_dirs(d, c);
     S *const pc = (S *)d.dd + c;
     const int64_t ps = d.pstride;
+    if (fl == kGhost) {  // lbm_alpha.cl:31-32; a sending ghost cell forwards its slots as they are
+        if (dirs) alpha_push<S>(d, c, dirs, [&](int f) { return pop_ld<S>(pc + f * ps, f); });
+        return;
+    }
     R f[19];
 #pragma unroll
     for (int i = 0; i < 19; i++) f[i] = pop_ld<S>(pc + i * ps, i);
     R r, vx, vy, vz;
-    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d)) {
+    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d, store_rho != 0)) {
         // each population goes to the opposite slot (lbm_alpha.cl:185-301)
 #pragma unroll
         for (int i = 0; i < 19; i++) pop_st<S>(pc + opp(i) * ps, f[i], opp(i));
+        if (dirs) alpha_push<S>(d, c, dirs, [&](int s) { return f[opp(s)]; });
+    } else if (dirs) {  // populations untouched
+        alpha_push<S>(d, c, dirs, [&](int s) { return f[s]; });
     }
     if (store_v) {
         R *u = (R *)d.vel + c;
@@ -897,7 +1019,7 @@ __device__ __forceinline__ void alpha_pair(const LatDesc &d, int64_t c, int stor
     constexpr bool DEV = Store<S>::kDev;
     P2 r, vx, vy, vz;
     if (fl0 == kFluid && fl1 == kFluid) {
-        alpha_phys<P2, LES, DEV>(kFluid, f, r, vx, vy, vz, d);
+        alpha_phys<P2, LES, DEV>(kFluid, f, r, vx, vy, vz, d, store_rho != 0);
 #pragma unroll
         for (int i = 0; i < 19; i++) pop_st2<S>(pc + opp(i) * ps, f[i], opp(i));
     } else {
@@ -909,7 +1031,7 @@ __device__ __forceinline__ void alpha_pair(const LatDesc &d, int64_t c, int stor
             R g[19], rr, ux, uy, uz;
 #pragma unroll
             for (int i = 0; i < 19; i++) g[i] = h ? f[i].y : f[i].x;
-            if (alpha_phys<R, LES, DEV>(fl, g, rr, ux, uy, uz, d)) {
+            if (alpha_phys<R, LES, DEV>(fl, g, rr, ux, uy, uz, d, store_rho != 0)) {
 #pragma unroll
                 for (int i = 0; i < 19; i++) pop_st<S>(pc + opp(i) * ps + h, g[i], opp(i));
             }
@@ -967,7 +1089,7 @@ static_assert(2 * kStages * 8 <= 64 && 64 + 4 * kStages <= 128, "the ring header
 __device__ unsigned int g_stage_error;
 
 template <typename S> struct Tile {
-    static_assert(sizeof(S) <= 4, "staged tiles hold float, half or bfloat16 populations");
+    static_assert(sizeof(S) <= 4, "staged tiles hold float or 16-bit populations");
     static constexpr int T = 1024 / (int)sizeof(S);  // cells per tile: 1 KB per plane
     static constexpr int A = 16 / (int)sizeof(S);    // elements per 16-byte boundary
     static constexpr int PER = (T + 32 * kConsumerWarps - 1) / (32 * kConsumerWarps);  // cells per compute thread
@@ -1101,15 +1223,31 @@ __device__ __forceinline__ void unstage_tile(const StepArgs<N> &a, int t, int li
     __syncwarp();
 }
 
+// Scatter target of population i of cell c: c + e_i in plane i.  W32: the
+// lattice's 19 planes span fewer than 2^32 elements (19 pstride < 2^32), so
+// the element offset from the buffer start is formed in 32-bit unsigned
+// arithmetic and widened once by the address computation; otherwise in
+// 64 bits.
+template <typename S, bool W32>
+__device__ __forceinline__ S *scatter_ptr(const LatDesc &d, int64_t c, int i) {
+    if constexpr (W32) {
+        const uint32_t nx = (uint32_t)d.nx, sl = (uint32_t)d.nx * (uint32_t)d.ny;
+        const uint32_t o = (uint32_t)c + (uint32_t)i * (uint32_t)d.pstride + (uint32_t)dir_x(i) +
+                           (uint32_t)dir_y(i) * nx + (uint32_t)dir_z(i) * sl;
+        return (S *)d.dd + o;
+    } else {
+        return (S *)d.dd + (c + (i * d.pstride + dir_off(i, (int64_t)d.nx, (int64_t)d.nx * d.ny)));
+    }
+}
+
 // One beta cell of an inside tile: sources from the ring buffer (the
 // offset (-e_i . (1, nx, nx ny)) mod A is -e_ix mod A because A divides
 // nx), results scattered to the neighbours.
-template <typename S, bool LES>
+template <typename S, bool LES, bool W32>
 __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
                                                  int store_v, int store_rho) {
     using TL = Tile<S>;
     using R = typename Store<S>::R;
-    const int64_t nx = d.nx, sl = (int64_t)d.nx * d.ny, ps = d.pstride;
     const int fl = stage[19 * TL::SEG + l];
     R f[19];
 #pragma unroll
@@ -1119,9 +1257,8 @@ __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigne
     }
     R r, vx, vy, vz;
     beta_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d);
-    S *const pc = (S *)d.dd + c;
 #pragma unroll
-    for (int i = 0; i < 19; i++) pop_st<S>(pc + (i * ps + dir_off(i, nx, sl)), f[i], i);
+    for (int i = 0; i < 19; i++) pop_st<S>(scatter_ptr<S, W32>(d, c, i), f[i], i);
     if (fl == kGhost) return;  // lbm_beta.cl:787-788
     if (store_v) {
         R *u = (R *)d.vel + c;
@@ -1138,14 +1275,12 @@ __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigne
 // two to a register meanwhile.  Used with the subgrid model (measured at
 // 512^3: f16 70.1k -> 73.6k MLUPS); without it the held halves push the
 // register-capped kernel into spills and the one-cell loop stays faster.
-template <typename S, bool LES>
+template <typename S, bool LES, bool W32>
 __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
                                                  int store_v, int store_rho) {
     using TL = Tile<S>;
     using R = typename Store<S>::R;
     static_assert(Store<S>::kDev, "pairs of 16-bit populations");
-    const int64_t nx = d.nx, sl = (int64_t)d.nx * d.ny, ps = d.pstride;
-    S *const pc = (S *)d.dd + c;
     uint32_t keep[5];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -1162,7 +1297,7 @@ __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigne
 #pragma unroll
         for (int i = 0; i < 19; i++) {
             if (dir_x(i) != 0) {
-                pop_st<S>(pc + (h + i * ps + dir_off(i, nx, sl)), f[i], i);
+                pop_st<S>(scatter_ptr<S, W32>(d, c + h, i), f[i], i);
                 continue;
             }
             const uint32_t bits = Store<S>::dbits(f[i]);
@@ -1170,7 +1305,7 @@ __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigne
                 keep[k >> 1] = (k & 1) ? (keep[k >> 1] | (bits << 16)) : bits;
             } else {
                 const uint32_t first = (k & 1) ? (keep[k >> 1] >> 16) : (keep[k >> 1] & 0xffffu);
-                *(uint32_t *)(pc + (i * ps + dir_off(i, nx, sl))) = first | (bits << 16);
+                *(uint32_t *)scatter_ptr<S, W32>(d, c, i) = first | (bits << 16);
             }
             k++;
         }
@@ -1194,7 +1329,7 @@ __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned cha
 #pragma unroll
     for (int i = 0; i < 19; i++) f[i] = pop_ld<S>((const S *)(stage + i * TL::SEG) + l, i);
     R r, vx, vy, vz;
-    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d)) {
+    if (alpha_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d, store_rho != 0)) {
 #pragma unroll
         for (int i = 0; i < 19; i++) pop_st<S>((S *)(stage + opp(i) * TL::SEG) + l, f[i], opp(i));
     }
@@ -1208,7 +1343,8 @@ __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned cha
 // N: descriptors in the parameter space (kParamLattices for domains and
 // single lattices; kBatchLattices for the alpha steps of an ensemble chunk
 // whose members are all at an alpha step).
-template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
+// W32: every lattice of the launch has 19 pstride < 2^32 (scatter_ptr).
+template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices, bool W32 = false>
 __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ StepArgs<N> a,
                                                                                   int tiles) {
     using TL = Tile<S>;
@@ -1282,14 +1418,14 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
         } else if constexpr (BETA && LES && Store<S>::kDev) {
 #pragma unroll 1
             for (int l = 2 * threadIdx.x; l < TL::T; l += 64 * kConsumerWarps)
-                beta_staged_pair<S, LES>(d, stage, l, c0 + l, a.store_v, a.store_rho);
+                beta_staged_pair<S, LES, W32>(d, stage, l, c0 + l, a.store_v, a.store_rho);
         } else {
 #pragma unroll 1
             for (int m = 0; m < TL::PER; m++) {
                 const int l = threadIdx.x + 32 * kConsumerWarps * m;
                 const int64_t c = c0 + l;
                 if (l >= TL::T || c >= d.n) break;
-                if (BETA) beta_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
+                if (BETA) beta_staged_cell<S, LES, W32>(d, stage, l, c, a.store_v, a.store_rho);
                 else alpha_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
             }
         }

@@ -2,7 +2,7 @@
 
     python -m turbulent_lbm_multigpu_gb300.experiments precision [--size 768 --steps 5000]
     python -m turbulent_lbm_multigpu_gb300.experiments batch [--count 512 --scale 1]
-    python -m turbulent_lbm_multigpu_gb300.experiments serve [--requests 64 --scale 1]
+    python -m turbulent_lbm_multigpu_gb300.experiments serve [--requests 256 --scale 1]
 
 Each prints one JSON object.  Inputs are synthetic and seeded: lid-driven
 cavities drawn with the seeds and distributions of the configurations
@@ -71,7 +71,7 @@ def centerline_ux(L: api.Lattice, layout: int):
 
 
 # ------------------------------------------------------------- precision
-def precision(size=768, steps=5000, every=100, compare_every=1000, storages=("f64", "f32", "f16", "bf16"),
+def precision(size=768, steps=5000, every=100, compare_every=1000, storages=("f64", "f32", "f16", "bf16", "c16"),
               re=20000.0, lid=0.1, seed=1234, amp=1e-3):
     dims = (size, size, size)
     tau = tau_for(lid, size, re)
@@ -121,6 +121,7 @@ def precision(size=768, steps=5000, every=100, compare_every=1000, storages=("f6
                       "amp": amp, "reference": ref},
            "mlups": {k: cells * steps / (v * 1e-3) / 1e6 for k, v in ms.items()},
            "final_error_vs_" + ref: errors[-1], "error_series": errors}
+    out["deviation_stats"] = {k: api.deviation_stats(L) for k, L in lats.items() if k in ("f16", "bf16", "c16")}
     layout = (steps - 1) & 1
     prof = {k: centerline_ux(L, layout) for k, L in lats.items()}
     out["centerline_ux"] = {k: {"mean": float(v.mean()), "rms": float(np.sqrt((v ** 2).mean())),
@@ -177,12 +178,31 @@ def batch(count=512, seed=42, scale=1.0, check=4):
             a, b = L.read(api.FIELD_DD), B.lattices[i].read(api.FIELD_DD)
             same = same and bool(np.array_equal(a.view(np.uint8), b.view(np.uint8)))
         del L
+    # one by one again, each cavity's steps replayed from a captured graph (a
+    # one-subdomain domain): separates the launch overhead from the packing
+    t_graph = 0.0
+    for i, c in enumerate(specs):
+        D = api.Domain((c.nx, c.ny, c.nz), (1, 1, 1), c.storage)
+        D.set_params(_lattice_params(c.storage, c.tau0, c.cs, c.lid))
+        D.reset()
+        D.perturb(c.seed, c.amp)
+        _sync()
+        t0 = time.perf_counter()
+        D.run(c.steps, use_graph=True)
+        _sync()
+        t_graph += time.perf_counter() - t0
+        if i < check:
+            a, b = D.subdomains[0].read(api.FIELD_DD), B.lattices[i].read(api.FIELD_DD)
+            same = same and bool(np.array_equal(a.view(np.uint8), b.view(np.uint8)))
+        D.close()
     return {"config": {"cavities": count, "seed": seed, "step_scale": scale, "cell_updates": updates,
                        "f16_share": sum(c.storage == api.F16 for c in specs) / count},
             "tuned_cells_per_thread": shape, "tune_ms_per_step": tune_ms,
             "batched_s": t_batch, "batched_mlups": updates / t_batch / 1e6,
             "one_by_one_s": t_seq, "one_by_one_mlups": updates / t_seq / 1e6,
-            "speedup": t_seq / t_batch, f"first_{check}_identical": same}
+            "one_by_one_graph_s": t_graph, "one_by_one_graph_mlups": updates / t_graph / 1e6,
+            "speedup": t_seq / t_batch, "speedup_vs_graph_replay": t_graph / t_batch,
+            f"first_{check}_identical": same}
 
 
 # ----------------------------------------------------------------- serving
@@ -200,33 +220,59 @@ def serve_specs(requests=64, seed=7, scale=1.0):
     return specs
 
 
-def serve_run(specs, rate, seed=7, budget=150e9, quantum=64):
+def serve_run(specs, rate, seed=7, budget=150e9, quantum=64, keep=()):
+    """Poisson arrivals at `rate` per second into the continuous-batching
+    server.  Per request: arrival, admission (the tick whose admission step
+    took it: the server admits in arrival order), completion.  The
+    populations and flags of the requests in `keep` are read back at
+    completion (for the accuracy check)."""
     rng = np.random.default_rng(seed + int(rate))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
     S = api.Server(budget, store_velocity=False)
-    lat = {}
     submitted = 0
+    waiting = []  # submitted, not yet admitted, in arrival order
     t0 = time.perf_counter()
-    done_at = {}
-    sid_of = {}
+    done_at, admit_at, sid_of, kept = {}, {}, {}, {}
+    ticks = 0
     while len(done_at) < len(specs):
         now = time.perf_counter() - t0
         while submitted < len(specs) and arrivals[submitted] <= now:
             sid_of[S.submit(specs[submitted])] = submitted
+            waiting.append(submitted)
             submitted += 1
-        if S.status()["active"] == 0 and S.status()["queued"] == 0:
+        st = S.status()
+        if st["active"] == 0 and st["queued"] == 0:
             # idle until the next arrival
             time.sleep(max(0.0, arrivals[submitted] - now))
             continue
-        S.tick(max_steps=quantum)
+        t_tick = time.perf_counter() - t0
+        n_adm = S.tick(max_steps=quantum)
+        ticks += 1
+        for i in waiting[:n_adm]:
+            admit_at[i] = t_tick
+        del waiting[:n_adm]
         for sid in S.poll():
-            done_at[sid_of[sid]] = time.perf_counter() - t0
+            i = sid_of[sid]
+            done_at[i] = time.perf_counter() - t0
+            if i in keep:
+                L = S.lattice(sid)
+                kept[i] = (L.read(api.FIELD_DD), L.read(api.FIELD_FLAGS)[0])
             S.release(sid)
     lat = np.array([done_at[i] - arrivals[i] for i in range(len(specs))])
+    wait = np.array([admit_at[i] - arrivals[i] for i in range(len(specs))]).clip(min=0.0)
+    service = np.array([done_at[i] - admit_at[i] for i in range(len(specs))])
     elapsed = max(done_at.values()) - arrivals[0]
+    admitted_span = max(admit_at.values()) - min(admit_at.values())
     updates = S.status()["cell_updates"]
-    return {"rate": rate, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "solves_per_s": len(specs) / elapsed, "mlups": updates / elapsed / 1e6, "elapsed_s": elapsed}
+    pct = lambda a, q: float(np.percentile(a, q))  # noqa: E731
+    out = {"rate": rate, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+           "queue_wait_p50_s": pct(wait, 50), "queue_wait_p99_s": pct(wait, 99),
+           "service_p50_s": pct(service, 50), "service_p99_s": pct(service, 99),
+           "offered_per_s": len(specs) / (arrivals[-1] - arrivals[0]),
+           "admitted_per_s": (len(specs) - 1) / admitted_span if admitted_span > 0 else float("inf"),
+           "solves_per_s": len(specs) / elapsed, "mlups": updates / elapsed / 1e6, "elapsed_s": elapsed,
+           "ticks": ticks}
+    return out, kept
 
 
 def sequential_plain(specs):
@@ -245,15 +291,70 @@ def sequential_plain(specs):
     return {"solves_per_s": len(specs) / t, "mlups": updates / t / 1e6, "elapsed_s": t}
 
 
-def serve(requests=64, seed=7, scale=1.0, rates=(50, 100, 200, 400), budget=150e9):
+_EXYZ = np.array([[1, -1, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0, 0, 0, 0],
+                  [0, 0, 1, -1, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 0],
+                  [0, 0, 0, 0, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 1, -1, 0]], dtype=np.float64)
+
+
+def _velocity_error(dd, dd_ref, flags):
+    """Relative RMS and max error of the momentum sum_i e_i f_i over the fluid
+    cells (both populations in the same slot layout)."""
+    m = flags == api.FLAG_FLUID
+    j = _EXYZ @ dd[:, m].astype(np.float64)
+    r = _EXYZ @ dd_ref[:, m].astype(np.float64)
+    d = np.sqrt(((j - r) ** 2).sum(0))
+    nr = np.sqrt((r ** 2).sum(0))
+    return {"rel_rms": float(np.sqrt((d ** 2).sum() / (nr ** 2).sum())), "rel_max": float(d.max() / nr.max())}
+
+
+def served_accuracy(specs, kept):
+    """Velocity error of served 16-bit solves (read back at completion)
+    against the same solve in FP64 alone, beside the error of the same solve
+    in plain FP32 alone."""
+    rows = []
+    for i, (dd, flags) in sorted(kept.items()):
+        c = specs[i]
+        ref = cavity_lattice((c.nx, c.ny, c.nz), api.F64, c.tau0, c.cs, c.lid, c.seed, c.amp)
+        ref.run(0, c.steps)
+        f64 = ref.read(api.FIELD_DD)
+        del ref
+        L32 = cavity_lattice((c.nx, c.ny, c.nz), api.F32, c.tau0, c.cs, c.lid, c.seed, c.amp)
+        L32.run(0, c.steps)
+        f32 = L32.read(api.FIELD_DD)
+        del L32
+        rows.append({"request": i, "dims": [c.nx, c.ny, c.nz], "steps": c.steps, "storage": int(c.storage),
+                     "served_vs_f64": _velocity_error(dd, f64, flags),
+                     "plain_f32_vs_f64": _velocity_error(f32, f64, flags)})
+    return rows
+
+
+def serve(requests=256, seed=7, scale=1.0, rates=(50, 100, 200, 400), budget=150e9, accuracy_samples=6,
+          f32_rate=100):
     specs = serve_specs(requests, seed, scale)
     seq = sequential_plain(specs)
-    runs = [serve_run(specs, r, seed, budget) for r in rates]
-    return {"config": {"requests": requests, "seed": seed, "step_scale": scale, "budget_bytes": budget,
-                       "f16_share": sum(c.storage == api.F16 for c in specs) / requests,
-                       "cell_updates": sum(c.nx * c.ny * c.nz * c.steps for c in specs)},
-            "sequential_plain_f32": seq, "served": runs,
-            "speedup_solves_per_s": [r["solves_per_s"] / seq["solves_per_s"] for r in runs]}
+    # the accuracy sample: the first 16-bit requests of at most ~2.1 M cells
+    keep = [i for i, c in enumerate(specs) if c.storage != api.F32 and c.nx * c.ny * c.nz <= 2_100_000]
+    keep = set(keep[:accuracy_samples])
+    runs, kept = [], {}
+    for r in rates:
+        out, k = serve_run(specs, r, seed, budget, keep=keep if r == rates[0] else ())
+        runs.append(out)
+        kept.update(k)
+    # the same requests all in plain f32, served: packing without the 16-bit share
+    specs32 = [api.Cavity.make((c.nx, c.ny, c.nz), api.F32, c.tau0, c.cs, c.lid, c.steps, c.seed, c.amp)
+               for c in specs]
+    out = {"config": {"requests": requests, "seed": seed, "step_scale": scale, "budget_bytes": budget,
+                      "f16_share": sum(c.storage == api.F16 for c in specs) / requests,
+                      "cell_updates": sum(c.nx * c.ny * c.nz * c.steps for c in specs)},
+           "sequential_plain_f32": seq, "served": runs,
+           "speedup_solves_per_s": [r["solves_per_s"] / seq["solves_per_s"] for r in runs]}
+    if f32_rate:
+        served32, _ = serve_run(specs32, f32_rate, seed, budget)
+        out["served_all_f32"] = served32
+        out["speedup_all_f32"] = served32["solves_per_s"] / seq["solves_per_s"]
+    if kept:
+        out["accuracy"] = served_accuracy(specs, kept)
+    return out
 
 
 def main():
@@ -262,7 +363,7 @@ def main():
     ap.add_argument("--size", type=int, default=768)
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--count", type=int, default=512)
-    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--scale", type=float, default=1.0)
     a = ap.parse_args()
     from . import build
