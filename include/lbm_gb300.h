@@ -124,9 +124,9 @@ int lbm_cu_step(lbm_lattice *lat, int parity, void *stream);
  * arithmetic type is float and nx is even, else 1.  3: persistent blocks
  * that stream tiles of cells through shared memory with TMA bulk copies (a
  * producer warp keeps the next tiles in flight while eight warps compute);
- * float, half and bfloat16 storage, else 1; the beta step of a lattice whose
+ * float and the 16-bit storage types, else 1; the beta step of a lattice whose
  * nx is not a multiple of 16 bytes of populations runs shape 1.  0
- * (default): 3 for half and bfloat16 storage, 1 for float and double, the
+ * (default): 3 for the 16-bit storage types, 1 for float and double, the
  * fastest measured on GB300.  All shapes give bit-identical results.  No
  * reference counterpart (the reference's work-group size list,
  * src/CLbmSolver.hpp:279-312, tunes its OpenCL launch instead). */
@@ -277,6 +277,18 @@ int lbm_cu_domain_set_fp64_contraction(lbm_domain *dom, int enable);
  * reference's -DPROFILE event timestamps (src/libcl/CCL.hpp:1752-1776). */
 int lbm_cu_domain_profile(lbm_domain *dom, int enable);
 int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launches, int reset);
+/* Capture the next `steps` steps (from the current step counter's parity)
+ * into one CUDA graph with an event pair around every step kernel, without
+ * running them.  While profiling is on (lbm_cu_domain_profile), the next
+ * lbm_cu_domain_run of exactly that many steps with use_graph != 0 from a
+ * counter of the same parity launches this graph, and
+ * lbm_cu_domain_kernel_time then reads its events: kernel times of a run
+ * replayed as a graph, without the launch gaps of step-by-step timing.
+ * Velocity and density, if stored, are written on the last step only (store
+ * interval 0).  Any change of the domain's parameters or kernel options
+ * drops the graph.  No reference counterpart (the reference times its steps
+ * with host clocks, src/CController.hpp:396-522). */
+int lbm_cu_domain_prepare_timed_run(lbm_domain *dom, int steps, void *stream);
 int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
 /* Step counter of the next lbm_cu_domain_run (its parity picks beta or alpha;
  * CLbmSolver::simulation_step_counter). */

@@ -439,3 +439,37 @@ def test_deviation_stats_match_the_stored_bits(capi, oracle_mod, storage):
         from test_oracle_pin import _c16_value
         dev = _c16_value(raw)
     assert got["max_abs"] == np.abs(dev).max()
+
+
+@pytest.mark.parametrize("storage,steps", [("f32", 7), ("f16", 6)])
+def test_timed_graph_run_equals_eager_steps(capi, storage, steps):
+    """lbm_cu_domain_prepare_timed_run: the captured run with an event pair
+    around every step kernel gives the bits of step-by-step launches and
+    times exactly `steps` kernels; a run of another length does not use it."""
+    api = capi
+    size, nums = (48, 32, 16), (2, 2, 1)
+
+    def made():
+        D = api.Domain(size, nums, api.STORAGE_NAMES[storage], True, True)
+        D.set_params(api.Params.make(1.0 / 0.56, 0.56, api.les_coefficient(0.17), (0, 0, 0), 0.08))
+        D.set_store_interval(0)
+        D.reset()
+        D.perturb(SEED, 1e-2)
+        D.run(3, use_graph=False)
+        return D
+
+    A, B = made(), made()
+    A.run(steps, use_graph=False)
+    B.profile(True)
+    B.kernel_time(reset=True)
+    B.prepare_timed_run(steps)
+    B.run(steps, use_graph=True)
+    ms, n = B.kernel_time(reset=True)
+    assert n == steps and ms > 0
+    assert B.counter == A.counter == 3 + steps
+    for La, Lb in zip(A.subdomains, B.subdomains):
+        for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY):
+            assert n_diff(La.read(f), Lb.read(f)) == 0
+    B.run(steps + 1, use_graph=True)  # another length: the ordinary path (step by step while profiling)
+    ms2, n2 = B.kernel_time(reset=True)
+    assert n2 == steps + 1

@@ -1186,6 +1186,13 @@ struct lbm_domain {
     int store_interval = 1;  // write u/rho every k-th step; 0 = last step of a run
     cudaGraphExec_t graph = nullptr;
     cudaStream_t cap_stream = nullptr;
+    // one captured graph of a whole timed run (lbm_cu_domain_prepare_timed_run):
+    // its steps, the counter parity it starts at, and an event pair around
+    // every step kernel, read by lbm_cu_domain_kernel_time after it ran
+    cudaGraphExec_t tgraph = nullptr;
+    int tgraph_steps = 0, tgraph_parity = 0;
+    bool tgraph_ran = false;
+    std::vector<cudaEvent_t> tev;
     // step-kernel timing with CUDA events (eager steps only)
     bool profile = false;
     std::vector<cudaEvent_t> ev;  // pairs: start, stop
@@ -1325,6 +1332,9 @@ int domain_one_step(lbm_domain *D, int parity, cudaStream_t st, bool store, bool
 void drop_graph(lbm_domain *D) {
     if (D->graph) cudaGraphExecDestroy(D->graph);
     D->graph = nullptr;
+    if (D->tgraph) cudaGraphExecDestroy(D->tgraph);
+    D->tgraph = nullptr;
+    D->tgraph_ran = false;
 }
 }  // namespace
 
@@ -1460,6 +1470,7 @@ int lbm_cu_domain_destroy(lbm_domain *D) {
     drop_graph(D);
     if (D->cap_stream) cudaStreamDestroy(D->cap_stream);
     for (cudaEvent_t e : D->ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : D->tev) cudaEventDestroy(e);
     if (D->owns)
         for (auto *l : D->subs) lbm_cu_destroy(l);
     delete D;
@@ -1504,11 +1515,65 @@ int lbm_cu_domain_perturb(lbm_domain *D, uint64_t seed, double amp, void *stream
     return 0;
 }
 
+int lbm_cu_domain_prepare_timed_run(lbm_domain *D, int steps, void *stream) {
+    if (!D) return fail("NULL domain");
+    if (steps < 1) return fail("a timed run has at least one step");
+    if (D->store_interval != 0 && (D->store_v || D->store_rho))
+        return fail("a timed run writes velocity and density on its last step only (store interval 0)");
+    if (domain_upload_tab(D, S(stream))) return -1;
+    if (D->tgraph) cudaGraphExecDestroy(D->tgraph);
+    D->tgraph = nullptr;
+    D->tgraph_ran = false;
+    while (D->tev.size() < 2 * (size_t)steps) {
+        cudaEvent_t e;
+        CU(cudaEventCreate(&e));
+        D->tev.push_back(e);
+    }
+    if (!D->cap_stream) CU(cudaStreamCreateWithFlags(&D->cap_stream, cudaStreamNonBlocking));
+    const bool les = uses_les(D->subs[0]->h);
+    cudaGraph_t g = nullptr;
+    CU(cudaStreamBeginCapture(D->cap_stream, cudaStreamCaptureModeThreadLocal));
+    bool ok = true;
+    for (int k = 0; k < steps && ok; k++) {
+        const int parity = (int)((D->counter + k) & 1);
+        const bool store = k + 1 == steps;
+        const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
+        ok = cudaEventRecordWithFlags(D->tev[2 * k], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
+        ok = ok && !launch_step(D->storage, D->eff_shape, parity, les, D->h_tab.data(), (int)D->subs.size(), sv, sr,
+                                D->cap_stream);
+        ok = ok && cudaEventRecordWithFlags(D->tev[2 * k + 1], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
+        for (int a = 0; a < 3 && ok; a++)
+            if (!D->plan[parity][a].empty() && !(parity == 1 && a == 0 && D->x_fused))
+                ok = !launch_halo_batch(D->storage, D->plan[parity][a].data(), (int)D->plan[parity][a].size(),
+                                        D->plan_cells[parity][a], D->plan_planes[parity][a], D->cap_stream);
+    }
+    const cudaError_t e = cudaStreamEndCapture(D->cap_stream, &g);
+    if (!ok || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(std::string("capturing the timed run: ") + (e != cudaSuccess ? cudaGetErrorString(e) : g_err));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&D->tgraph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        D->tgraph = nullptr;
+        return fail(std::string("graph instantiate: ") + cudaGetErrorString(ei));
+    }
+    D->tgraph_steps = steps;
+    D->tgraph_parity = (int)(D->counter & 1);
+    return 0;
+}
+
 int lbm_cu_domain_run(lbm_domain *D, int steps, int use_graph, void *stream) {
     if (!D) return fail("NULL domain");
     if (steps < 0) return fail("negative step count");
     cudaStream_t st = S(stream);
-    if (domain_upload_tab(D, st)) return -1;
+    if (domain_upload_tab(D, st)) return -1;  // may drop a timed graph captured with other descriptors
+    if (D->tgraph && use_graph && D->profile && steps == D->tgraph_steps && (int)(D->counter & 1) == D->tgraph_parity) {
+        CU(cudaGraphLaunch(D->tgraph, st));
+        D->counter += steps;
+        D->tgraph_ran = true;
+        return 0;
+    }
     int done = 0;
     // u/rho are written on steps whose new counter is a multiple of the
     // interval, or (interval 0) on the last step of this call
@@ -1622,6 +1687,16 @@ int lbm_cu_domain_profile(lbm_domain *D, int enable) {
 
 int lbm_cu_domain_kernel_time(lbm_domain *D, double *ms_total, int64_t *launches, int reset) {
     if (!D) return fail("NULL domain");
+    if (D->tgraph_ran) {
+        for (int k = 0; k < D->tgraph_steps; k++) {
+            CU(cudaEventSynchronize(D->tev[2 * k + 1]));
+            float ms = 0.f;
+            CU(cudaEventElapsedTime(&ms, D->tev[2 * k], D->tev[2 * k + 1]));
+            D->kernel_ms += ms;
+            D->kernel_launches++;
+        }
+        D->tgraph_ran = false;
+    }
     for (size_t i = 0; i + 1 < D->ev_used; i += 2) {
         CU(cudaEventSynchronize(D->ev[i + 1]));
         float ms = 0.f;
