@@ -278,17 +278,19 @@ int lbm_cu_domain_set_fp64_contraction(lbm_domain *dom, int enable);
 int lbm_cu_domain_profile(lbm_domain *dom, int enable);
 int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launches, int reset);
 /* Capture the next `steps` steps (from the current step counter's parity)
- * into one CUDA graph with an event pair around every step kernel, without
- * running them.  While profiling is on (lbm_cu_domain_profile), the next
- * lbm_cu_domain_run of exactly that many steps with use_graph != 0 from a
- * counter of the same parity launches this graph, and
- * lbm_cu_domain_kernel_time then reads its events: kernel times of a run
- * replayed as a graph, without the launch gaps of step-by-step timing.
- * Velocity and density, if stored, are written on the last step only (store
- * interval 0).  Any change of the domain's parameters or kernel options
- * drops the graph.  No reference counterpart (the reference times its steps
- * with host clocks, src/CController.hpp:396-522). */
-int lbm_cu_domain_prepare_timed_run(lbm_domain *dom, int steps, void *stream);
+ * into one CUDA graph without running them, with an event pair around the
+ * step kernels of steps k with k % every < 2 (every = 1: all of them; every
+ * event record in the graph costs about 1 % at 256^3 in 2x2x1 subdomains, so
+ * a sample of beta/alpha pairs times the kernels at a smaller cost).  While
+ * profiling is on (lbm_cu_domain_profile), the next lbm_cu_domain_run of
+ * exactly that many steps with use_graph != 0 from a counter of the same
+ * parity launches this graph, and lbm_cu_domain_kernel_time then reads its
+ * events: kernel times of a run replayed as a graph.  Velocity and density,
+ * if stored, are written on the last step only (store interval 0).  Any
+ * change of the domain's parameters or kernel options drops the graph.  No
+ * reference counterpart (the reference times its steps with host clocks,
+ * src/CController.hpp:396-522). */
+int lbm_cu_domain_prepare_timed_run(lbm_domain *dom, int steps, int every, void *stream);
 int lbm_cu_domain_counter(const lbm_domain *dom, int64_t *counter);
 /* Step counter of the next lbm_cu_domain_run (its parity picks beta or alpha;
  * CLbmSolver::simulation_step_counter). */

@@ -110,7 +110,7 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_set_kernel_shape": ([vp, ci], ci),
         "lbm_cu_domain_profile": ([vp, ci], ci),
         "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
-        "lbm_cu_domain_prepare_timed_run": ([vp, ci, vp], ci),
+        "lbm_cu_domain_prepare_timed_run": ([vp, ci, ci, vp], ci),
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
         "lbm_cu_domain_lattice": ([vp, ci], vp),
         "lbm_cu_run": ([vp, i64, i64, vp], ci),
@@ -396,10 +396,11 @@ class Domain:
         check(lib().lbm_cu_domain_kernel_time(self.h, C.byref(ms), C.byref(n), int(reset)))
         return ms.value, n.value
 
-    def prepare_timed_run(self, steps, stream=None):
-        """Capture the next `steps` steps as one graph with events around every
-        step kernel (run it with run(steps, use_graph=True) while profiling)."""
-        check(lib().lbm_cu_domain_prepare_timed_run(self.h, int(steps), stream))
+    def prepare_timed_run(self, steps, every=1, stream=None):
+        """Capture the next `steps` steps as one graph with events around the
+        step kernels of steps k % every < 2 (run it with run(steps,
+        use_graph=True) while profiling)."""
+        check(lib().lbm_cu_domain_prepare_timed_run(self.h, int(steps), int(every), stream))
 
 
 class Batch:

@@ -1190,7 +1190,7 @@ struct lbm_domain {
     // its steps, the counter parity it starts at, and an event pair around
     // every step kernel, read by lbm_cu_domain_kernel_time after it ran
     cudaGraphExec_t tgraph = nullptr;
-    int tgraph_steps = 0, tgraph_parity = 0;
+    int tgraph_steps = 0, tgraph_parity = 0, tgraph_every = 1;
     bool tgraph_ran = false;
     std::vector<cudaEvent_t> tev;
     // step-kernel timing with CUDA events (eager steps only)
@@ -1515,9 +1515,14 @@ int lbm_cu_domain_perturb(lbm_domain *D, uint64_t seed, double amp, void *stream
     return 0;
 }
 
-int lbm_cu_domain_prepare_timed_run(lbm_domain *D, int steps, void *stream) {
+// Steps of a timed run whose step kernel an event pair brackets: the pair of
+// steps (a beta and an alpha step) at the start of every `every` steps.
+static bool timed_step(int k, int every) { return k % every < 2; }
+
+int lbm_cu_domain_prepare_timed_run(lbm_domain *D, int steps, int every, void *stream) {
     if (!D) return fail("NULL domain");
     if (steps < 1) return fail("a timed run has at least one step");
+    if (every < 1) return fail("the sampling interval of a timed run is at least 1");
     if (D->store_interval != 0 && (D->store_v || D->store_rho))
         return fail("a timed run writes velocity and density on its last step only (store interval 0)");
     if (domain_upload_tab(D, S(stream))) return -1;
@@ -1538,10 +1543,12 @@ int lbm_cu_domain_prepare_timed_run(lbm_domain *D, int steps, void *stream) {
         const int parity = (int)((D->counter + k) & 1);
         const bool store = k + 1 == steps;
         const int sv = store ? D->store_v : 0, sr = store ? D->store_rho : 0;
-        ok = cudaEventRecordWithFlags(D->tev[2 * k], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
+        const bool timed = timed_step(k, every);
+        if (timed) ok = cudaEventRecordWithFlags(D->tev[2 * k], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
         ok = ok && !launch_step(D->storage, D->eff_shape, parity, les, D->h_tab.data(), (int)D->subs.size(), sv, sr,
                                 D->cap_stream);
-        ok = ok && cudaEventRecordWithFlags(D->tev[2 * k + 1], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
+        if (timed)
+            ok = ok && cudaEventRecordWithFlags(D->tev[2 * k + 1], D->cap_stream, cudaEventRecordExternal) == cudaSuccess;
         for (int a = 0; a < 3 && ok; a++)
             if (!D->plan[parity][a].empty() && !(parity == 1 && a == 0 && D->x_fused))
                 ok = !launch_halo_batch(D->storage, D->plan[parity][a].data(), (int)D->plan[parity][a].size(),
@@ -1559,6 +1566,7 @@ int lbm_cu_domain_prepare_timed_run(lbm_domain *D, int steps, void *stream) {
         return fail(std::string("graph instantiate: ") + cudaGetErrorString(ei));
     }
     D->tgraph_steps = steps;
+    D->tgraph_every = every;
     D->tgraph_parity = (int)(D->counter & 1);
     return 0;
 }
@@ -1689,6 +1697,7 @@ int lbm_cu_domain_kernel_time(lbm_domain *D, double *ms_total, int64_t *launches
     if (!D) return fail("NULL domain");
     if (D->tgraph_ran) {
         for (int k = 0; k < D->tgraph_steps; k++) {
+            if (!timed_step(k, D->tgraph_every)) continue;
             CU(cudaEventSynchronize(D->tev[2 * k + 1]));
             float ms = 0.f;
             CU(cudaEventElapsedTime(&ms, D->tev[2 * k], D->tev[2 * k + 1]));
