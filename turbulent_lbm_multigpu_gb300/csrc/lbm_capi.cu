@@ -521,7 +521,7 @@ static int sm_count() {
     return cache[dev];
 }
 
-template <typename S, bool LES, bool BETA, bool ONE, int N, bool W32>
+template <typename S, bool LES, bool BETA, bool ONE, int N, int ADDR>
 static int launch_staged_w(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     // the ring exceeds the default 48 KB of dynamic shared memory; the limit
     // is raised once per device
@@ -530,27 +530,44 @@ static int launch_staged_w(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     CU(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail("device index out of range");
     if (!attr[dev]) {
-        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N, W32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CU(cudaFuncSetAttribute(k_step_staged<S, LES, BETA, ONE, N, ADDR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 Tile<S>::SMEM));
         attr[dev] = true;
     }
     const int grid = std::min(tiles, sm_count() * kStageBlocksPerSM);
-    k_step_staged<S, LES, BETA, ONE, N, W32><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
+    k_step_staged<S, LES, BETA, ONE, N, ADDR><<<grid, kStageThreads, Tile<S>::SMEM, st>>>(a, tiles);
     CU(cudaGetLastError());
     return 0;
 }
 
 // Beta steps whose lattices all span fewer than 2^32 population elements
-// form their scatter addresses in 32-bit arithmetic (scatter_ptr).
+// form their scatter addresses in 32-bit arithmetic (scatter_ptr): from a
+// table of the 19 offsets when the lattices share their shape (domains and
+// single lattices), else computed per lattice (ensembles).
 template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices>
 static int launch_staged_one(const StepArgs<N> &a, int tiles, cudaStream_t st) {
     if constexpr (BETA) {
-        bool w32 = true;
-        for (int i = 0; i < a.ntab; i++)
+        bool w32 = true, same = true;
+        for (int i = 0; i < a.ntab; i++) {
             if (19 * a.tab[i].pstride >= ((int64_t)1 << 32)) w32 = false;
-        if (w32) return launch_staged_w<S, LES, BETA, ONE, N, true>(a, tiles, st);
+            if (a.tab[i].nx != a.tab[0].nx || a.tab[i].ny != a.tab[0].ny || a.tab[i].pstride != a.tab[0].pstride)
+                same = false;
+        }
+        if constexpr (N == kParamLattices) {
+            if (w32 && same) {
+                StepArgs<N> b = a;
+                const uint32_t nx = (uint32_t)a.tab[0].nx, sl = nx * (uint32_t)a.tab[0].ny;
+                for (int i = 0; i < 19; i++)
+                    b.koff[i] = (uint32_t)i * (uint32_t)a.tab[0].pstride + (uint32_t)dir_x(i) +
+                                (uint32_t)dir_y(i) * nx + (uint32_t)dir_z(i) * sl;
+                return launch_staged_w<S, LES, BETA, ONE, N, kAddrTab>(b, tiles, st);
+            }
+        } else {
+            (void)same;
+            if (w32) return launch_staged_w<S, LES, BETA, ONE, N, kAddr32>(a, tiles, st);
+        }
     }
-    return launch_staged_w<S, LES, BETA, ONE, N, false>(a, tiles, st);
+    return launch_staged_w<S, LES, BETA, ONE, N, kAddr64>(a, tiles, st);
 }
 
 template <typename S, bool LES, bool BETA>

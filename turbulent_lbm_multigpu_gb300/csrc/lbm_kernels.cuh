@@ -312,6 +312,11 @@ template <int N> struct StepArgs {
     const int32_t *block_lattice;  // lattice of every block of the launch, or null
     int ntab;
     int store_v, store_rho;
+    // Element offsets i pstride + e_i . (1, nx, nx ny) (mod 2^32) of the beta
+    // scatter targets, when every lattice of the launch shares nx, ny and the
+    // plane stride (the subdomains of a domain, a single lattice): set for
+    // the staged beta's table addressing (kAddrTab), else unused.
+    uint32_t koff[19];
 };
 using DomainArgs = StepArgs<kParamLattices>;
 using BatchArgs = StepArgs<kBatchLattices>;
@@ -1223,14 +1228,18 @@ __device__ __forceinline__ void unstage_tile(const StepArgs<N> &a, int t, int li
     __syncwarp();
 }
 
-// Scatter target of population i of cell c: c + e_i in plane i.  W32: the
-// lattice's 19 planes span fewer than 2^32 elements (19 pstride < 2^32), so
-// the element offset from the buffer start is formed in 32-bit unsigned
-// arithmetic and widened once by the address computation; otherwise in
-// 64 bits.
-template <typename S, bool W32>
-__device__ __forceinline__ S *scatter_ptr(const LatDesc &d, int64_t c, int i) {
-    if constexpr (W32) {
+// Scatter target of population i of cell c: c + e_i in plane i.  When the
+// lattice's 19 planes span fewer than 2^32 elements (19 pstride < 2^32) the
+// element offset from the buffer start is formed in 32-bit unsigned
+// arithmetic and widened once by the address computation: from the
+// launch's offset table (kAddrTab, lattices of equal shape) or computed
+// (kAddr32); otherwise in 64 bits (kAddr64).
+enum : int { kAddr64 = 0, kAddr32 = 1, kAddrTab = 2 };
+template <typename S, int ADDR>
+__device__ __forceinline__ S *scatter_ptr(const LatDesc &d, int64_t c, int i, const uint32_t *koff) {
+    if constexpr (ADDR == kAddrTab) {
+        return (S *)d.dd + ((uint32_t)c + koff[i]);
+    } else if constexpr (ADDR == kAddr32) {
         const uint32_t nx = (uint32_t)d.nx, sl = (uint32_t)d.nx * (uint32_t)d.ny;
         const uint32_t o = (uint32_t)c + (uint32_t)i * (uint32_t)d.pstride + (uint32_t)dir_x(i) +
                            (uint32_t)dir_y(i) * nx + (uint32_t)dir_z(i) * sl;
@@ -1243,9 +1252,9 @@ __device__ __forceinline__ S *scatter_ptr(const LatDesc &d, int64_t c, int i) {
 // One beta cell of an inside tile: sources from the ring buffer (the
 // offset (-e_i . (1, nx, nx ny)) mod A is -e_ix mod A because A divides
 // nx), results scattered to the neighbours.
-template <typename S, bool LES, bool W32>
+template <typename S, bool LES, int ADDR>
 __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
-                                                 int store_v, int store_rho) {
+                                                 int store_v, int store_rho, const uint32_t *koff) {
     using TL = Tile<S>;
     using R = typename Store<S>::R;
     const int fl = stage[19 * TL::SEG + l];
@@ -1258,7 +1267,7 @@ __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigne
     R r, vx, vy, vz;
     beta_phys<R, LES, Store<S>::kDev>(fl, f, r, vx, vy, vz, d);
 #pragma unroll
-    for (int i = 0; i < 19; i++) pop_st<S>(scatter_ptr<S, W32>(d, c, i), f[i], i);
+    for (int i = 0; i < 19; i++) pop_st<S>(scatter_ptr<S, ADDR>(d, c, i, koff), f[i], i);
     if (fl == kGhost) return;  // lbm_beta.cl:787-788
     if (store_v) {
         R *u = (R *)d.vel + c;
@@ -1275,9 +1284,9 @@ __device__ __forceinline__ void beta_staged_cell(const LatDesc &d, const unsigne
 // two to a register meanwhile.  Used with the subgrid model (measured at
 // 512^3: f16 70.1k -> 73.6k MLUPS); without it the held halves push the
 // register-capped kernel into spills and the one-cell loop stays faster.
-template <typename S, bool LES, bool W32>
+template <typename S, bool LES, int ADDR>
 __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigned char *stage, int l, int64_t c,
-                                                 int store_v, int store_rho) {
+                                                 int store_v, int store_rho, const uint32_t *koff) {
     using TL = Tile<S>;
     using R = typename Store<S>::R;
     static_assert(Store<S>::kDev, "pairs of 16-bit populations");
@@ -1297,7 +1306,7 @@ __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigne
 #pragma unroll
         for (int i = 0; i < 19; i++) {
             if (dir_x(i) != 0) {
-                pop_st<S>(scatter_ptr<S, W32>(d, c + h, i), f[i], i);
+                pop_st<S>(scatter_ptr<S, ADDR>(d, c + h, i, koff), f[i], i);
                 continue;
             }
             const uint32_t bits = Store<S>::dbits(f[i]);
@@ -1305,7 +1314,7 @@ __device__ __forceinline__ void beta_staged_pair(const LatDesc &d, const unsigne
                 keep[k >> 1] = (k & 1) ? (keep[k >> 1] | (bits << 16)) : bits;
             } else {
                 const uint32_t first = (k & 1) ? (keep[k >> 1] >> 16) : (keep[k >> 1] & 0xffffu);
-                *(uint32_t *)scatter_ptr<S, W32>(d, c, i) = first | (bits << 16);
+                *(uint32_t *)scatter_ptr<S, ADDR>(d, c, i, koff) = first | (bits << 16);
             }
             k++;
         }
@@ -1343,8 +1352,8 @@ __device__ __forceinline__ void alpha_staged_cell(const LatDesc &d, unsigned cha
 // N: descriptors in the parameter space (kParamLattices for domains and
 // single lattices; kBatchLattices for the alpha steps of an ensemble chunk
 // whose members are all at an alpha step).
-// W32: every lattice of the launch has 19 pstride < 2^32 (scatter_ptr).
-template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices, bool W32 = false>
+// ADDR: how the beta step forms its scatter addresses (scatter_ptr).
+template <typename S, bool LES, bool BETA, bool ONE, int N = kParamLattices, int ADDR = kAddr64>
 __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_staged(const __grid_constant__ StepArgs<N> a,
                                                                                   int tiles) {
     using TL = Tile<S>;
@@ -1418,14 +1427,14 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
         } else if constexpr (BETA && LES && Store<S>::kDev) {
 #pragma unroll 1
             for (int l = 2 * threadIdx.x; l < TL::T; l += 64 * kConsumerWarps)
-                beta_staged_pair<S, LES, W32>(d, stage, l, c0 + l, a.store_v, a.store_rho);
+                beta_staged_pair<S, LES, ADDR>(d, stage, l, c0 + l, a.store_v, a.store_rho, a.koff);
         } else {
 #pragma unroll 1
             for (int m = 0; m < TL::PER; m++) {
                 const int l = threadIdx.x + 32 * kConsumerWarps * m;
                 const int64_t c = c0 + l;
                 if (l >= TL::T || c >= d.n) break;
-                if (BETA) beta_staged_cell<S, LES, W32>(d, stage, l, c, a.store_v, a.store_rho);
+                if (BETA) beta_staged_cell<S, LES, ADDR>(d, stage, l, c, a.store_v, a.store_rho, a.koff);
                 else alpha_staged_cell<S, LES>(d, stage, l, c, a.store_v, a.store_rho);
             }
         }
