@@ -240,7 +240,7 @@ def make_params(api, storage):
 
 
 def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, shape=None, halo_mode=HALO_MODE,
-            fp64_fma=False):
+            fp64_fma=False, fused=True):
     """K timed steps of one domain, replayed as one captured CUDA graph with a
     CUDA-event pair around every step kernel; returns (ms of the K steps,
     step-kernel ms per launch, MLUPS of the same K steps launched one by one
@@ -254,6 +254,8 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, sha
         D.set_kernel_shape(shape)
     if fp64_fma:
         D.set_fp64_contraction(True)
+    if not fused:
+        D.set_fused_exchange(False)
     D.reset()
     D.perturb(SEED, AMP)
     D.run(warmup, use_graph=False)
@@ -273,6 +275,7 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, sha
         stop.record()
         torch.cuda.synchronize()
     ms = start.elapsed_time(stop)
+    (b_ms, b_n), (a_ms, a_n) = D.kernel_time_by_step()
     k_ms, k_n = D.kernel_time(reset=True)
     want = sum(1 for k in range(steps) if k % TIMED_EVERY < 2)
     if k_n != want:
@@ -286,6 +289,7 @@ def measure(api, size, nums, storage, steps, warmup, dist=None, clocks=None, sha
     cells = D.cells
     eager_mlups = cells * steps / (g0.elapsed_time(g1) * 1e-3) / 1e6
     del D
+    measure.split = (b_ms / max(1, b_n), a_ms / max(1, a_n))  # beta, alpha ms per launch
     return ms, k_ms / max(1, k_n), eager_mlups, cells
 
 
@@ -313,6 +317,7 @@ def run_gpu(args):
     with ClockSampler(local) as clk:
         ms, k_ms, eager_mlups, cells = measure(api, args.size, args.nums, args.storage, args.steps, args.warmup, dist,
                                                shape=args.shape, fp64_fma=args.fp64_fma)
+        beta_ms, alpha_ms = measure.split
     ms = max_over_ranks(ms, dist)
     mlups = whole_job_mlups(cells, args.steps, ms, ws)
     if args.steps < 2:
@@ -332,7 +337,11 @@ def run_gpu(args):
                 "frac": round(achieved / peak, 4), "traffic": round(traffic * cells) if traffic else None,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6.8 TB/s", "kernel": kname,
-                "kernel_ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": alg_bytes}
+                "kernel_ms_per_launch": round(k_ms, 4), "alg_bytes_per_launch": alg_bytes,
+                "by_step": {"beta_ms": round(beta_ms, 4), "beta_frac": round(alg_bytes / (beta_ms * 1e-3) / 1e9 / peak, 4),
+                            "alpha_ms": round(alpha_ms, 4),
+                            "alpha_frac": round(alg_bytes / (alpha_ms * 1e-3) / 1e9 / peak, 4),
+                            "note": "the alpha kernel also copies the x faces of the exchange that follows it"}}
 
     prm = make_params(api, "f32")
     e2e = None if args.no_e2e else run_e2e(api, prm, args.steps)
@@ -340,19 +349,22 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra and tuple(args.size) == SIZE:
         n = max(50, min(args.steps, 400))
-        for label, size, nums, st, hm, fma in (
-                ("f32 256^3 2x2x1, reference exchange (19 populations after alpha)", SIZE, NUMS, "f32", 0, False),
-                ("f64 256^3 2x2x1", SIZE, NUMS, "f64", HALO_MODE, False),
-                ("f64 256^3 2x2x1, contracted multiply-adds (<= 1e-12 per step)", SIZE, NUMS, "f64", HALO_MODE, True),
-                ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16", HALO_MODE, False),
-                ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16", HALO_MODE, False),
-                ("c16-shifted 256^3 2x2x1 (13-bit significand)", SIZE, NUMS, "c16", HALO_MODE, False),
-                ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32", HALO_MODE, False),
-                ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16", HALO_MODE, False),
-                ("c16-shifted 512^3", (512, 512, 512), (1, 1, 1), "c16", HALO_MODE, False)):
-            xms, xk, xg, xc = measure(api, size, nums, st, n, 4, halo_mode=hm, fp64_fma=fma)
+        for label, size, nums, st, hm, fma, fu in (
+                ("f32 256^3 2x2x1, x faces after alpha in their own launch", SIZE, NUMS, "f32", HALO_MODE, False, False),
+                ("f32 256^3 2x2x1, reference exchange (19 populations after alpha)", SIZE, NUMS, "f32", 0, False, True),
+                ("f64 256^3 2x2x1", SIZE, NUMS, "f64", HALO_MODE, False, True),
+                ("f64 256^3 2x2x1, contracted multiply-adds (<= 1e-12 per step)", SIZE, NUMS, "f64", HALO_MODE, True, True),
+                ("f16-shifted 256^3 2x2x1", SIZE, NUMS, "f16", HALO_MODE, False, True),
+                ("bf16-shifted 256^3 2x2x1", SIZE, NUMS, "bf16", HALO_MODE, False, True),
+                ("c16-shifted 256^3 2x2x1 (13-bit significand)", SIZE, NUMS, "c16", HALO_MODE, False, True),
+                ("f32 512^3", (512, 512, 512), (1, 1, 1), "f32", HALO_MODE, False, True),
+                ("f16-shifted 512^3", (512, 512, 512), (1, 1, 1), "f16", HALO_MODE, False, True),
+                ("c16-shifted 512^3", (512, 512, 512), (1, 1, 1), "c16", HALO_MODE, False, True)):
+            xms, xk, xg, xc = measure(api, size, nums, st, n, 4, halo_mode=hm, fp64_fma=fma, fused=fu)
             xa = BYTES_PER_CELL[st] * xc / (xk * 1e-3) / 1e9
+            xb, xa_ = measure.split
             extra[label] = {"mlups": round(xc * n / (xms * 1e-3) / 1e6, 1), "eager_mlups": round(xg, 1),
+                            "beta_ms": round(xb, 4), "alpha_ms": round(xa_, 4),
                             "kernel_ms": round(xk, 4), "achieved_gbs": round(xa, 1),
                             "frac_of_measured_hbm": round(xa / peak, 4), "steps": n,
                             "alg_bytes_per_cell": BYTES_PER_CELL[st]}

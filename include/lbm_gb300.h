@@ -277,6 +277,9 @@ int lbm_cu_domain_set_fp64_contraction(lbm_domain *dom, int enable);
  * reference's -DPROFILE event timestamps (src/libcl/CCL.hpp:1752-1776). */
 int lbm_cu_domain_profile(lbm_domain *dom, int enable);
 int lbm_cu_domain_kernel_time(lbm_domain *dom, double *ms_total, int64_t *launches, int reset);
+/* The same times split by step kind: index 0 beta steps (even counter),
+ * 1 alpha steps (odd counter). */
+int lbm_cu_domain_kernel_time_by_step(lbm_domain *dom, double ms[2], int64_t launches[2], int reset);
 /* Capture the next `steps` steps (from the current step counter's parity)
  * into one CUDA graph without running them, with an event pair around the
  * step kernels of steps k with k % every < 2 (every = 1: all of them; every

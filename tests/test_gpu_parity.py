@@ -445,7 +445,8 @@ def test_deviation_stats_match_the_stored_bits(capi, oracle_mod, storage):
 def test_timed_graph_run_equals_eager_steps(capi, storage, steps, every):
     """lbm_cu_domain_prepare_timed_run: the captured run with an event pair
     around every step kernel gives the bits of step-by-step launches and
-    times exactly `steps` kernels; a run of another length does not use it."""
+    times exactly `steps` kernels, split into beta and alpha steps; a run of
+    another length does not use it."""
     api = capi
     size, nums = (48, 32, 16), (2, 2, 1)
 
@@ -464,8 +465,13 @@ def test_timed_graph_run_equals_eager_steps(capi, storage, steps, every):
     B.kernel_time(reset=True)
     B.prepare_timed_run(steps, every)
     B.run(steps, use_graph=True)
+    (b_ms, b_n), (a_ms, a_n) = B.kernel_time_by_step()
     ms, n = B.kernel_time(reset=True)
     assert n == sum(1 for k in range(steps) if k % every < 2) and ms > 0
+    # step k runs on counter 3 + k: beta on an even counter, alpha on an odd one
+    assert b_n == sum(1 for k in range(steps) if k % every < 2 and (3 + k) % 2 == 0)
+    assert a_n == n - b_n and b_ms > 0 and a_ms > 0
+    assert abs(b_ms + a_ms - ms) <= 1e-9 * max(1.0, ms)
     assert B.counter == A.counter == 3 + steps
     for La, Lb in zip(A.subdomains, B.subdomains):
         for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY):

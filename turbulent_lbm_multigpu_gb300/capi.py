@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
         "lbm_cu_domain_profile": ([vp, ci], ci),
         "lbm_cu_domain_kernel_time": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
         "lbm_cu_domain_prepare_timed_run": ([vp, ci, ci, vp], ci),
+        "lbm_cu_domain_kernel_time_by_step": ([vp, C.POINTER(cd), C.POINTER(i64), ci], ci),
         "lbm_cu_domain_subdomains": ([vp, ip, ip], ci),
         "lbm_cu_domain_lattice": ([vp, ci], vp),
         "lbm_cu_run": ([vp, i64, i64, vp], ci),
@@ -395,6 +396,12 @@ class Domain:
         ms, n = C.c_double(), C.c_int64()
         check(lib().lbm_cu_domain_kernel_time(self.h, C.byref(ms), C.byref(n), int(reset)))
         return ms.value, n.value
+
+    def kernel_time_by_step(self, reset=False):
+        """((beta ms, launches), (alpha ms, launches)) of the timed step kernels."""
+        ms, n = (C.c_double * 2)(), (C.c_int64 * 2)()
+        check(lib().lbm_cu_domain_kernel_time_by_step(self.h, ms, n, int(reset)))
+        return (ms[0], n[0]), (ms[1], n[1])
 
     def prepare_timed_run(self, steps, every=1, stream=None):
         """Capture the next `steps` steps as one graph with events around the

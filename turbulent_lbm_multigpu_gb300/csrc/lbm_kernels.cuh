@@ -311,6 +311,10 @@ template <int N> struct StepArgs {
     LatDesc tab[N];
     const int32_t *block_lattice;  // lattice of every block of the launch, or null
     int ntab;
+    // Nonzero: the lattices have equal block counts and their blocks are
+    // interleaved, block b running block b / ntab of lattice b % ntab, so
+    // that the same rows of all subdomains are in flight together.
+    int interleave;
     int store_v, store_rho;
     // Element offsets i pstride + e_i . (1, nx, nx ny) (mod 2^32) of the beta
     // scatter targets, when every lattice of the launch shares nx, ny and the
@@ -327,7 +331,9 @@ static_assert(sizeof(BatchArgs) + sizeof(int) <= 32764, "kernel parameters excee
 template <int N>
 __device__ __forceinline__ const LatDesc &lattice_of(const StepArgs<N> &a) {
     int li = 0;
-    if (a.block_lattice) {
+    if (a.interleave) {
+        li = (int)(blockIdx.x % (unsigned)a.ntab);
+    } else if (a.block_lattice) {
         li = a.block_lattice[blockIdx.x];
     } else if (a.ntab > 1) {
         int hi = a.ntab - 1;
@@ -337,6 +343,12 @@ __device__ __forceinline__ const LatDesc &lattice_of(const StepArgs<N> &a) {
         }
     }
     return a.tab[li];
+}
+
+// Index of this block within its lattice (see StepArgs::interleave).
+template <int N>
+__device__ __forceinline__ int64_t block_in_lattice(const StepArgs<N> &a, const LatDesc &d) {
+    return a.interleave ? (int64_t)(blockIdx.x / (unsigned)a.ntab) : (int64_t)blockIdx.x - d.first_block;
 }
 
 // ------------------------------------------------------------- equilibria
@@ -805,7 +817,7 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
 template <typename S, bool LES>
 __global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_beta(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
-    const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
+    const int64_t c0 = block_in_lattice(a, d) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
     if (c >= d.n) return;
     const int64_t reach = (int64_t)d.nx + (int64_t)d.nx * d.ny;
@@ -889,7 +901,7 @@ __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int stor
 template <typename S, bool LES>
 __global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_alpha(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
-    const int64_t c = (int64_t)(blockIdx.x - d.first_block) * blockDim.x + threadIdx.x;
+    const int64_t c = block_in_lattice(a, d) * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
     alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
 }
