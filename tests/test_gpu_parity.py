@@ -384,7 +384,7 @@ def test_fused_x_exchange_equals_separate_launch(capi, size, nums, halo_mode):
     """The x part of the exchange after alpha done by the one-cell alpha
     kernel itself gives the same bits as its own copy launch: subdomains of
     three cells in x (the x = 1 cells send both ways), 64 subdomains, the
-    benchmark's subdomain width."""
+    benchmark's subdomain width; runs ending on a beta and on an alpha step."""
     api = capi
 
     def run(fused):
@@ -395,13 +395,50 @@ def test_fused_x_exchange_equals_separate_launch(capi, size, nums, halo_mode):
         D.reset()
         D.perturb(SEED, 1e-2)
         D.run(5, use_graph=False)
+        out = [[L.read(api.FIELD_DD) for L in D.subdomains]]
         D.set_store_interval(0)
-        D.run(8, use_graph=True)
-        return [[L.read(f) for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY)] for L in D.subdomains]
+        for steps in (8, 3):
+            D.run(steps, use_graph=True)
+            out.append([L.read(f) for L in D.subdomains for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY)])
+        return out
 
     for a, b in zip(run(True), run(False)):
         for x, y in zip(a, b):
             assert n_diff(x, y) == 0
+
+
+@pytest.mark.parametrize("nums", [(2, 1, 1), (2, 2, 2)])
+def test_fused_exchange_with_obstacles_at_the_interface(capi, nums):
+    """Obstacle cells next to an x interface, whose alpha steps leave their
+    populations alone but still send the x faces to the neighbour's ghost
+    layer: the alpha kernel's copies give the bits of the copy launches;
+    runs ending on an alpha and on a beta step."""
+    api = capi
+    size = (24, 16, 12)
+    sub = [s // n for s, n in zip(size, nums)]
+
+    def run(fused):
+        D = api.Domain(size, nums, api.F32, True, True)
+        D.set_params(api.Params.make(1.0 / 0.53, 0.53, api.les_coefficient(0.17), (0, 0, 0), 0.08))
+        D.set_fused_exchange(fused)
+        D.reset()
+        D.perturb(SEED, 1e-2)
+        box = (2, min(4, sub[1] - 3), min(3, sub[2] - 2))
+        for i, L in enumerate(D.subdomains):
+            x0 = 1 if (i % nums[0]) else sub[0] - 3  # next to the interface on both sides
+            L.write(api.FIELD_FLAGS, np.full(box[0] * box[1] * box[2], api.FLAG_OBSTACLE, np.int32),
+                    origin=(x0, 1, 1), size=box)
+        out = []
+        for steps, graph in ((4, False), (7, False), (6, True), (5, True)):
+            D.run(steps, use_graph=graph)
+            out.append([[L.read(f) for f in (api.FIELD_DD, api.FIELD_VELOCITY, api.FIELD_DENSITY)]
+                        for L in D.subdomains])
+        return out
+
+    for a, b in zip(run(True), run(False)):
+        for sa, sb in zip(a, b):
+            for x, y in zip(sa, sb):
+                assert n_diff(x, y) == 0
 
 
 @pytest.mark.parametrize("storage", ["f16", "bf16", "c16"])
