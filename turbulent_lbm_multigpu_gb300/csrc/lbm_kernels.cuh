@@ -771,12 +771,24 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
 }
 
 // Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
-// registers) for the one-cell float kernels with the subgrid model, 3 (80)
-// without it (its straight-line code schedules with more live values), 1
-// for double.
-template <typename S, bool LES>
+// registers) for the one-cell float-arithmetic kernels with the subgrid
+// model, 3 (80) without it (its straight-line code schedules with more live
+// values), 1 for double.  Over float populations the step kernels are bound
+// by the loads each warp keeps in flight (a warp loads, then computes for
+// about twice the load latency with nothing in flight), so they take the
+// most blocks that compile without spilling: the alpha kernel fits 48
+// registers with or without the subgrid model and runs 5 (subgrid model,
+// 256^3 in 2x2x1 subdomains: 447 -> 424 us; 512^3: 3.32 -> 3.15 ms, 95 % of
+// the measured copy bandwidth; without it 478 -> 406 us), the beta kernel
+// without the subgrid model fits 64 and runs 4 (at 80 registers it spilled).
+// The beta kernel with the subgrid model spills at 48 and ran slower there
+// (415 -> 452 us), so it keeps 4.  KIND: 0 any, 1 alpha, 2 beta.
+template <typename S, bool LES, int KIND = 0>
 __host__ __device__ constexpr int min_blocks() {
-    return sizeof(typename Store<S>::R) == 8 ? 1 : LES ? 4 : 3;
+    if (sizeof(typename Store<S>::R) == 8) return 1;
+    if (KIND == 1 && sizeof(S) == 4) return 5;
+    if (KIND == 2 && sizeof(S) == 4) return 4;
+    return LES ? 4 : 3;
 }
 
 // ---------------------------------------------------- one cell per thread
@@ -815,7 +827,7 @@ __device__ __forceinline__ void beta_cell(const LatDesc &d, int64_t c, int store
 }
 
 template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_beta(const __grid_constant__ DomainArgs a) {
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, 2>())) k_beta(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
     const int64_t c0 = block_in_lattice(a, d) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
@@ -899,7 +911,7 @@ __device__ __forceinline__ void alpha_cell(const LatDesc &d, int64_t c, int stor
 }
 
 template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_alpha(const __grid_constant__ DomainArgs a) {
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, 1>())) k_alpha(const __grid_constant__ DomainArgs a) {
     const LatDesc &d = lattice_of(a);
     const int64_t c = block_in_lattice(a, d) * blockDim.x + threadIdx.x;
     if (c >= d.n) return;
