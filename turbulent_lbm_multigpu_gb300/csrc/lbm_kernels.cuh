@@ -773,7 +773,9 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
 // Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
 // registers) for the one-cell float-arithmetic kernels with the subgrid
 // model, 3 (80) without it (its straight-line code schedules with more live
-// values), 1 for double.  Over float populations the step kernels are bound
+// values); for double arithmetic 3 (85 registers) for the alpha kernel and 2
+// (128) for the others, the most that compile without spilling (at the
+// compiler's own choice, 122-140 registers, one block fit per SM).  Over float populations the step kernels are bound
 // by the loads each warp keeps in flight (a warp loads, then computes for
 // about twice the load latency with nothing in flight), so they take the
 // most blocks that compile without spilling: the alpha kernel fits 48
@@ -785,7 +787,7 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
 // (415 -> 452 us), so it keeps 4.  KIND: 0 any, 1 alpha, 2 beta.
 template <typename S, bool LES, int KIND = 0>
 __host__ __device__ constexpr int min_blocks() {
-    if (sizeof(typename Store<S>::R) == 8) return 1;
+    if (sizeof(typename Store<S>::R) == 8) return KIND == 1 ? 3 : 2;
     if (KIND == 1 && sizeof(S) == 4) return 5;
     if (KIND == 2 && sizeof(S) == 4) return 4;
     return LES ? 4 : 3;
