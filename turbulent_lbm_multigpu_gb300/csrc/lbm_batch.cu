@@ -31,12 +31,26 @@ using namespace lbm_rt;
 namespace lbm_rt {
 
 template <typename S, bool PAIR>
-int launch_tick_t(bool les, const BatchArgs &a, int blocks, int j, cudaStream_t st) {
+int launch_tick_t(bool les, const BatchArgs &a, int blocks, int j, int uni, cudaStream_t st) {
     if (blocks <= 0) return 0;
     if constexpr (PAIR) {
         if (les) k_step2<S, true><<<blocks, kBlock, 0, st>>>(a, j);
         else k_step2<S, false><<<blocks, kBlock, 0, st>>>(a, j);
+    } else if constexpr (sizeof(S) >= 4) {
+        // float and double chunks whose cavities are all at the same kind of
+        // step run that kind's kernel alone (its own launch bounds)
+        if (uni == 1) {
+            if (les) k_step<S, true, 1><<<blocks, kBlock, 0, st>>>(a, j);
+            else k_step<S, false, 1><<<blocks, kBlock, 0, st>>>(a, j);
+        } else if (uni == 2) {
+            if (les) k_step<S, true, 2><<<blocks, kBlock, 0, st>>>(a, j);
+            else k_step<S, false, 2><<<blocks, kBlock, 0, st>>>(a, j);
+        } else {
+            if (les) k_step<S, true><<<blocks, kBlock, 0, st>>>(a, j);
+            else k_step<S, false><<<blocks, kBlock, 0, st>>>(a, j);
+        }
     } else {
+        (void)uni;
         if (les) k_step<S, true><<<blocks, kBlock, 0, st>>>(a, j);
         else k_step<S, false><<<blocks, kBlock, 0, st>>>(a, j);
     }
@@ -44,22 +58,22 @@ int launch_tick_t(bool les, const BatchArgs &a, int blocks, int j, cudaStream_t 
     return 0;
 }
 
-int launch_tick(int storage, bool pair, bool les, const BatchArgs &a, int blocks, int j, cudaStream_t st) {
+int launch_tick(int storage, bool pair, bool les, const BatchArgs &a, int blocks, int j, int uni, cudaStream_t st) {
     if (pair) {
         switch (storage) {
-            case kF32: return launch_tick_t<float, true>(les, a, blocks, j, st);
-            case kF16: return launch_tick_t<__half, true>(les, a, blocks, j, st);
-            case kBF16: return launch_tick_t<__nv_bfloat16, true>(les, a, blocks, j, st);
-            case kC16: return launch_tick_t<c16_t, true>(les, a, blocks, j, st);
+            case kF32: return launch_tick_t<float, true>(les, a, blocks, j, uni, st);
+            case kF16: return launch_tick_t<__half, true>(les, a, blocks, j, uni, st);
+            case kBF16: return launch_tick_t<__nv_bfloat16, true>(les, a, blocks, j, uni, st);
+            case kC16: return launch_tick_t<c16_t, true>(les, a, blocks, j, uni, st);
         }
         return fail("the two-cell kernels need a float arithmetic type");
     }
     switch (storage) {
-        case kF32: return launch_tick_t<float, false>(les, a, blocks, j, st);
-        case kF64: return launch_tick_t<double, false>(les, a, blocks, j, st);
-        case kF16: return launch_tick_t<__half, false>(les, a, blocks, j, st);
-        case kBF16: return launch_tick_t<__nv_bfloat16, false>(les, a, blocks, j, st);
-        case kC16: return launch_tick_t<c16_t, false>(les, a, blocks, j, st);
+        case kF32: return launch_tick_t<float, false>(les, a, blocks, j, uni, st);
+        case kF64: return launch_tick_t<double, false>(les, a, blocks, j, uni, st);
+        case kF16: return launch_tick_t<__half, false>(les, a, blocks, j, uni, st);
+        case kBF16: return launch_tick_t<__nv_bfloat16, false>(les, a, blocks, j, uni, st);
+        case kC16: return launch_tick_t<c16_t, false>(les, a, blocks, j, uni, st);
     }
     return fail("unknown storage type");
 }
@@ -272,7 +286,8 @@ struct Ensemble {
                 }
                 ch.args->store_v = store ? store_v : 0;
                 ch.args->store_rho = 0;
-                if (launch_tick(g.storage, g.pair, ch.les, *ch.args, ch.blocks, j, st)) return -1;
+                if (launch_tick(g.storage, g.pair, ch.les, *ch.args, ch.blocks, j, all_alpha ? 1 : all_beta ? 2 : 0, st))
+                    return -1;
             }
         return 0;
     }

@@ -1475,13 +1475,16 @@ __global__ void __launch_bounds__(kStageThreads, kStageBlocksPerSM) k_step_stage
 // a beta step for a lattice whose counter was even at the tick start and j
 // even (and so on), chosen per block.  Used for ensembles of cavities and
 // for the serving loop, where solves start at different times.
-template <typename S, bool LES>
-__global__ void __launch_bounds__(256, (min_blocks<S, LES>())) k_step(const __grid_constant__ BatchArgs a, int j) {
+// UNI: 0 each lattice at its own kind of step; 1 every lattice at an alpha
+// step, 2 at a beta step (the other kind's code compiled out, and the launch
+// bounds of that kind: min_blocks).
+template <typename S, bool LES, int UNI = 0>
+__global__ void __launch_bounds__(256, (min_blocks<S, LES, UNI>())) k_step(const __grid_constant__ BatchArgs a, int j) {
     const LatDesc &d = lattice_of(a);
     const int64_t c0 = (int64_t)(blockIdx.x - d.first_block) * blockDim.x;
     const int64_t c = c0 + threadIdx.x;
     if (c >= d.n) return;
-    if ((d.parity + j) & 1) {
+    if (UNI == 1 || (UNI == 0 && ((d.parity + j) & 1))) {
         alpha_cell<S, LES>(d, c, a.store_v, a.store_rho);
         return;
     }
