@@ -770,21 +770,19 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
     return i;
 }
 
-// Resident blocks of 256 threads per SM the launch bounds ask for: 4 (64
-// registers) for the one-cell float-arithmetic kernels with the subgrid
-// model, 3 (80) without it (its straight-line code schedules with more live
-// values); for double arithmetic 3 (85 registers) for the alpha kernel and 2
-// (128) for the others, the most that compile without spilling (at the
-// compiler's own choice, 122-140 registers, one block fit per SM).  Over float populations the step kernels are bound
-// by the loads each warp keeps in flight (a warp loads, then computes for
-// about twice the load latency with nothing in flight), so they take the
-// most blocks that compile without spilling: the alpha kernel fits 48
-// registers with or without the subgrid model and runs 5 (subgrid model,
-// 256^3 in 2x2x1 subdomains: 447 -> 424 us; 512^3: 3.32 -> 3.15 ms, 95 % of
-// the measured copy bandwidth; without it 478 -> 406 us), the beta kernel
-// without the subgrid model fits 64 and runs 4 (at 80 registers it spilled).
-// The beta kernel with the subgrid model spills at 48 and ran slower there
-// (415 -> 452 us), so it keeps 4.  KIND: 0 any, 1 alpha, 2 beta.
+// Resident blocks of 256 threads per SM the launch bounds ask for.  The
+// step kernels wait on the loads each warp keeps in flight (a warp loads,
+// then computes for about twice the load latency with nothing in flight),
+// so they take the most blocks that compile without spilling:
+//   float populations: alpha 5 (48 registers, with or without the subgrid
+//     model; 256^3 in 2x2x1 subdomains 447 -> 424 us, 512^3 3.32 -> 3.15 ms,
+//     95 % of the measured copy bandwidth; without the subgrid model
+//     478 -> 406 us), beta 4 (64; without the subgrid model it spilled at
+//     80; with it, it spills at 48 and ran slower there, 415 -> 452 us);
+//   double arithmetic: alpha 3 (85 registers), the others 2 (128); at the
+//     compiler's own choice, 122-140 registers, one block fit per SM;
+//   otherwise 4 (64) with the subgrid model, 3 (80) without it.
+// KIND: 0 any step, 1 alpha, 2 beta.
 template <typename S, bool LES, int KIND = 0>
 __host__ __device__ constexpr int min_blocks() {
     if (sizeof(typename Store<S>::R) == 8) return KIND == 1 ? 3 : 2;
