@@ -778,7 +778,8 @@ __device__ __forceinline__ int64_t wrap_cell(int64_t c, int64_t off, int64_t n) 
 //     model; 256^3 in 2x2x1 subdomains 447 -> 424 us, 512^3 3.32 -> 3.15 ms,
 //     95 % of the measured copy bandwidth; without the subgrid model
 //     478 -> 406 us), beta 4 (64; without the subgrid model it spilled at
-//     80; with it, it spills at 48 and ran slower there, 415 -> 452 us);
+//     80; with it, it spills at 48 and ran slower there, 415 -> 452 us, and
+//     at 56 in blocks of 128, 9 per SM, 413 -> 425 us);
 //   double arithmetic: alpha 3 (85 registers), the others 2 (128); at the
 //     compiler's own choice, 122-140 registers, one block fit per SM;
 //   otherwise 4 (64) with the subgrid model, 3 (80) without it.
